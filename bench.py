@@ -1,0 +1,486 @@
+#!/usr/bin/env python
+"""Benchmark: forward + backward DRR frames/s on one GB300.
+
+Workload (one "step" = one batch of poses through the render and its adjoint):
+a registration step on the seeded CT phantom — 512 x 512 x 512 float32
+volume (0.8 x 0.8 x 1.0 mm voxels), 32 poses (ZXY rotations uniform ±30°,
+translations ±50 mm about a source 600 mm from the isocenter), 256 x 256
+detector at 1.2 mm, SDD 1020 mm, 800 samples per ray; loss = NCC against
+target DRRs rendered at held-out poses; backward to the se(3) 6-vector of
+every pose and to the volume. One frame = one pose's image forward + backward.
+
+Arms:
+  default           the CUDA kernels (this package);
+  --impl reference  the reference's CPU path (its PyTorch grid_sample backend,
+                    restated in oracle/) on the host cores, on a bounded
+                    sample of the same workload.
+
+Prints one JSON line (rank 0). Under torchrun every rank renders its own
+pose batch against its own copy of the volume (no collective on the data
+path; weak scaling); the timed region is bracketed by barriers and the max
+over ranks is reported.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import torch  # noqa: E402
+
+BASELINE_HEADLINE = None  # the benchmark spec publishes no number for this metric
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--volume", default="512x512x512", help="DxHxW voxels")
+    p.add_argument("--spacing", default="0.8,0.8,1.0", help="sx,sy,sz mm")
+    p.add_argument("--batch", type=int, default=32)
+    p.add_argument("--det", type=int, default=256)
+    p.add_argument("--pixel", type=float, default=1.2)
+    p.add_argument("--samples", type=int, default=800)
+    p.add_argument("--cpu-rays", type=int, default=2048, help="rays per CPU-baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+# ------------------------------------------------------------------ helpers
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling in the background (200 ms)."""
+
+    FIELDS = (
+        "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+        "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+        "clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.TemporaryFile(mode="w+")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200",
+                 "-i", str(self.index)],
+                stdout=self.file, stderr=subprocess.DEVNULL,
+            )
+        except Exception:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.seek(0)
+        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.count(",") >= 6]
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[0]))
+                smax = float(r[1])
+            except ValueError:
+                continue
+            for name, v in zip(names, r[3:7]):
+                if v.strip().lower() == "active":
+                    reasons.add(name)
+        load = [s for s in sm if smax and s > 0.5 * smax] or sm
+        return {
+            "sm_mhz": statistics.median(load) if load else None,
+            "sm_max_mhz": smax,
+            "reasons": sorted(reasons),
+            "samples": len(sm),
+        }
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int, device) -> float:
+    if world == 1:
+        return x
+    import torch.distributed as dist
+
+    t = torch.tensor([x], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def parse_shape(s):
+    return tuple(int(v) for v in s.lower().split("x"))
+
+
+def workload(args, device, seed_offset=0):
+    """Phantom subject, detector, base poses, perturbation pivots and targets."""
+    from nanodrr_gb300 import phantom
+
+    D, H, W = parse_shape(args.volume)
+    sp = tuple(float(v) for v in args.spacing.split(","))
+    gen_dev = device if torch.cuda.is_available() else "cpu"
+    ph = phantom.make_phantom((D, H, W), sp, seed=0, device=gen_dev)
+    k_inv, sdd = phantom.detector(sdd=1020.0, pixel=args.pixel, height=args.det, width=args.det)
+    rt = phantom.random_poses(args.batch, seed=1 + seed_offset)
+    # held-out targets: the same poses perturbed by up to 0.05 rad / 5 mm
+    held = _nudge(rt, seed=77 + seed_offset)
+    return ph, k_inv, sdd, rt, held
+
+
+def _nudge(rt, seed):
+    from nanodrr_gb300.geometry import convert
+
+    g = torch.Generator().manual_seed(seed)
+    rot = (torch.rand(rt.shape[0], 3, generator=g) * 2 - 1) * 0.05
+    xyz = (torch.rand(rt.shape[0], 3, generator=g) * 2 - 1) * 5.0
+    return rt @ convert(rot, xyz, "so3_log")
+
+
+# --------------------------------------------------------------- our arm
+def count_samples(M, src, tgt, D, H, W, S):
+    """Samples inside each ray's march window (same rule as the kernel)."""
+    p0 = torch.einsum("bij,bnj->bni", M[:, :, :3], src.expand_as(tgt)) + M[:, None, :, 3]
+    d = torch.einsum("bij,bnj->bni", M[:, :, :3], tgt - src)
+    lo_b = torch.tensor([-2.0, -2.0, -2.0], device=M.device)
+    hi_b = torch.tensor([W + 1.0, H + 1.0, D + 1.0], device=M.device)
+    dd = torch.where(d.abs() < 1e-20, torch.full_like(d, 1e-20), d)
+    a = (lo_b - p0) / dd
+    b = (hi_b - p0) / dd
+    t_lo = torch.minimum(a, b).amax(-1)
+    t_hi = torch.maximum(a, b).amin(-1)
+    f_lo = (torch.floor(t_lo * (S - 1)) - 2).clamp(0, S)
+    f_hi = (torch.ceil(t_hi * (S - 1)) + 3).clamp(0, S)
+    n = (f_hi - f_lo).clamp(min=0)
+    n = torch.where(t_lo <= t_hi, n, torch.zeros_like(n))
+    return float(n.sum())
+
+
+def run_ours(args, world, rank, local):
+    import nanodrr_gb300 as nd
+    from nanodrr_gb300 import _build
+    from nanodrr_gb300.raymarch import raymarch_backward, raymarch_forward
+    from nanodrr_gb300.registration import NormalizedCrossCorrelation2d, Registration
+    from nanodrr_gb300.renderer import _make_src, _make_tgt
+
+    _build.build()
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    ph, k_inv, sdd, rt, held = workload(args, dev, seed_offset=rank)
+    sub = ph.subject(device=dev)
+    del ph
+    vol_param = sub._image_hu.detach().requires_grad_(True)
+    sub._image_hu = vol_param
+    k_inv, sdd, rt, held = k_inv.to(dev), sdd.to(dev), rt.to(dev), held.to(dev)
+    B, Hd, S = args.batch, args.det, args.samples
+    with torch.no_grad():
+        target = nd.render(sub, k_inv, held, sdd, Hd, Hd, n_samples=S)
+    ncc = NormalizedCrossCorrelation2d()
+    reg = Registration(sub, rt, k_inv, sdd, Hd, Hd, batch=B).to(dev)
+
+    def step():
+        vol_param.grad = None
+        reg._rot.grad = None
+        reg._xyz.grad = None
+        img = reg(n_samples=S)
+        loss = -ncc(img, target).mean()
+        loss.backward()
+        return loss
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- device-timed steps (inputs resident in HBM)
+    clocks = ClockSampler(torch.cuda.current_device())
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record()
+    for _ in range(args.steps):
+        step()
+    ev1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    t_dev = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, world, dev)
+    frames = B * args.steps * world
+    value = frames / t_dev
+
+    # ---- end to end through the public API: per step the pose 6-vectors
+    # come from pinned host memory and the loss + pose gradients go back.
+    host_params = torch.zeros(B, 6, pin_memory=True)
+    host_out = torch.zeros(1 + B * 6, pin_memory=True)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        with torch.no_grad():
+            p = host_params.to(dev, non_blocking=True)
+            reg._rot.copy_(p[:, :3])
+            reg._xyz.copy_(p[:, 3:])
+        loss = step()
+        res = torch.cat([loss.detach()[None], reg._rot.grad.flatten(), reg._xyz.grad.flatten()])
+        host_out.copy_(res, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+    t_e2e = max_over_ranks(time.perf_counter() - t0, world, dev)
+    barrier(world)
+    e2e = {
+        "value": frames / t_e2e,
+        "unit": "frames/s",
+        "h2d_bytes_per_step": host_params.numel() * 4,
+        "d2h_bytes_per_step": host_out.numel() * 4,
+    }
+
+    # ---- per-kernel timing for the roofline (same inputs, on the launch stream)
+    with torch.no_grad():
+        pose = reg.pose.detach()
+        M = (sub.world_to_voxel @ pose)[:, :3].contiguous()
+        tgt = _make_tgt(k_inv, sdd, Hd, Hd, dev, torch.float32).expand(B, -1, -1).contiguous()
+        src = _make_src(False, tgt, sdd.expand(B)).contiguous()
+        stepsz = ((tgt - src).norm(dim=-1) / (S - 1)).contiguous()
+        vol = sub.image[0, 0].detach()
+        D, H, W = vol.shape
+        go = torch.randn(B, 1, Hd * Hd, device=dev)
+        n_samp = count_samples(M, src, tgt, D, H, W, S)
+        gvol = torch.zeros_like(vol)
+        reps = max(3, args.steps)
+        fwd_ms, bwd_ms = [], []
+        for i in range(reps + 1):
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            e[0].record()
+            raymarch_forward(vol, vol, M, src, tgt, stepsz, S, 1, Hd)
+            e[1].record()
+            e[2].record()
+            raymarch_backward(go, vol, vol, M, src, tgt, stepsz, S, 1, Hd, True, True, gvol=gvol)
+            e[3].record()
+            torch.cuda.synchronize()
+            if i > 0:
+                fwd_ms.append(e[0].elapsed_time(e[1]))
+                bwd_ms.append(e[2].elapsed_time(e[3]))
+    e_bytes = vol.element_size()
+    fwd_bytes = n_samp * 8 * e_bytes
+    bwd_bytes = n_samp * (8 * e_bytes + 4 + 8 * 4 * 2)
+    fwd_s, bwd_s = statistics.median(fwd_ms) / 1e3, statistics.median(bwd_ms) / 1e3
+    peaks = _peaks()
+    dominant = ("bwd", bwd_bytes, bwd_s) if bwd_s >= fwd_s else ("fwd", fwd_bytes, fwd_s)
+    achieved = dominant[1] / dominant[2] / 1e9
+    roofline = {
+        "bound": "hbm",
+        "kernel": f"raymarch_{dominant[0]}_kernel",
+        "achieved": round(achieved, 1),
+        "peak": peaks["hbm_gbs"],
+        "peak_source": peaks["source"],
+        "unit": "GB/s",
+        "frac": round(achieved / peaks["hbm_gbs"], 4),
+        "traffic": None,
+        "algorithmic_bytes_per_launch": dominant[1],
+        "samples_per_launch": n_samp,
+        "fwd_ms": round(fwd_s * 1e3, 3),
+        "bwd_ms": round(bwd_s * 1e3, 3),
+        "fwd_gsamples_per_s": round(n_samp / fwd_s / 1e9, 2),
+        "bwd_gsamples_per_s": round(n_samp / bwd_s / 1e9, 2),
+    }
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, sub, k_inv, sdd, rt)
+    out = {
+        "metric": "fwd+bwd DRR frames/s at 512^3/256^2 (plain CUDA kernel)",
+        "value": round(value, 2),
+        "unit": "frames/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": max(args.warmup, 3),
+        "ms_per_step": round(t_dev / args.steps * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": BASELINE_HEADLINE,
+        "dtype": "f32",
+        "data": "synthetic seeded CT phantom (no dataset)",
+        "config": {
+            "workload": (
+                f"registration step: {args.volume} f32 phantom ({args.spacing} mm), {B} poses x "
+                f"{Hd}x{Hd} detector ({args.pixel} mm), {S} samples/ray, fwd + NCC + bwd to se(3) "
+                "6-vector and volume"
+            ),
+            "method": "plain kernel (box-culled march)",
+            "l2": "inputs larger than L2 (volume and its gradient 512 MiB each)",
+            "parallelism": f"replicas x{world}",
+        },
+        "samples_per_s": round(n_samp * args.steps * world / t_dev, 1),
+        "roofline": roofline,
+        "e2e": e2e,
+        "gpu_launches": 3 * args.steps,
+        "clocks": clk,
+    }
+    if cpu is not None:
+        out["cpu_baseline"] = cpu
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    except Exception:
+        return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+# ----------------------------------------------------------- CPU baseline
+def _cpu_sample(args, vol_cpu, w2v, k_inv, sdd, rt, rays):
+    """One bounded sample: `rays` rays of pose 0, forward + backward to the pose
+    and the volume through the restated reference CPU path (fp32)."""
+    from oracle import make_src, make_tgt, render_oracle
+
+    Hd = args.det
+    tgt_full = make_tgt(k_inv.cpu(), sdd.cpu(), Hd, Hd, torch.float32)
+    g = torch.Generator().manual_seed(0)
+    idx = torch.randperm(Hd * Hd, generator=g)[:rays]
+    tgt = tgt_full[:, idx]
+    src = make_src(False, tgt, sdd.cpu())
+    rtp = rt[:1].cpu().clone().requires_grad_(True)
+    vol = vol_cpu
+    vol.grad = None
+    out = render_oracle(vol, None, w2v, rtp, src, tgt, args.samples, 1)
+    out.sum().backward()
+    return out
+
+
+def cpu_baseline(args, sub, k_inv, sdd, rt):
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    vol_cpu = sub.image[0, 0].detach().float().cpu().requires_grad_(True)
+    w2v = sub.world_to_voxel.detach().float().cpu()
+    rays = args.cpu_rays
+    _cpu_sample(args, vol_cpu, w2v, k_inv, sdd, rt, max(64, rays // 8))  # warm-up
+    times = []
+    t_end = time.perf_counter() + 15.0
+    while len(times) < 3 or (time.perf_counter() < t_end and len(times) < 10):
+        t0 = time.perf_counter()
+        _cpu_sample(args, vol_cpu, w2v, k_inv, sdd, rt, rays)
+        times.append(time.perf_counter() - t0)
+    t = statistics.median(times)
+    frames_per_s = (rays / (args.det * args.det)) / t
+    return {
+        "value": round(frames_per_s, 4),
+        "unit": "frames/s",
+        "cores": threads,
+        "kind": "port",
+        "sample": (
+            f"{rays} of {args.det * args.det} rays of one pose, {args.samples} samples, fp32 forward + backward to "
+            f"pose and volume via torch grid_sample on CPU (the reference's PyTorch backend restated), median of "
+            f"{len(times)}; frames/s = ray fraction / time"
+        ),
+    }
+
+
+def run_reference(args, world, rank, local):
+    if rank != 0:
+        return
+    dev = torch.device("cuda", local) if torch.cuda.is_available() else torch.device("cpu")
+    ph, k_inv, sdd, rt, held = workload(args, dev)
+    sub = ph.subject(device="cpu")
+    del ph
+    threads = os.cpu_count() or 1
+    torch.set_num_threads(threads)
+    vol_cpu = sub.image[0, 0].detach().float().requires_grad_(True)
+    w2v = sub.world_to_voxel.float()
+    rays = args.cpu_rays
+    for _ in range(max(args.warmup, 1)):
+        _cpu_sample(args, vol_cpu, w2v, k_inv, sdd, rt, rays)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        _cpu_sample(args, vol_cpu, w2v, k_inv, sdd, rt, rays)
+        times.append(time.perf_counter() - t0)
+    total = sum(times)
+    frames = args.steps * rays / (args.det * args.det)
+    value = frames / total
+    out = {
+        "metric": "fwd+bwd DRR frames/s at 512^3/256^2 (plain CUDA kernel)",
+        "impl": "reference",
+        "value": round(value, 4),
+        "unit": "frames/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total / args.steps * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic seeded CT phantom (no dataset)",
+        "config": {
+            "workload": (
+                f"registration step: {args.volume} f32 phantom ({args.spacing} mm), {args.det}x{args.det} detector, "
+                f"{args.samples} samples/ray, fwd + bwd to pose and volume"
+            ),
+            "sample_per_step": f"{rays} rays of one pose",
+        },
+        "cpu_baseline": {
+            "value": round(value, 4),
+            "unit": "frames/s",
+            "cores": threads,
+            "kind": "port",
+            "sample": f"{rays} rays x {args.samples} samples per step, torch grid_sample on CPU (reference PyTorch "
+            "backend restated)",
+        },
+        "e2e": {"value": round(value, 4), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank, local)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

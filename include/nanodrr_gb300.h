@@ -1,0 +1,165 @@
+/*
+ * nanodrr_gb300 — C ABI of the GB300 (sm_103a) differentiable ray-march renderer.
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream handle
+ * (a `cudaStream_t` passed as `void*`; NULL is the legacy default stream). No
+ * entry point allocates device memory, synchronises the stream or calls into a
+ * framework: scratch memory is passed in by the caller, sized by the matching
+ * `*_workspace_bytes` query. All launches are asynchronous on `stream`.
+ *
+ * Return value: NDRR_OK (0) or one of the NDRR_ERR_* codes below; the message
+ * of the last failure on the calling thread is returned by ndrr_last_error().
+ *
+ * Coordinate conventions (identical to the reference renderer):
+ *   - the volume is a dense row-major [D, H, W] array; voxel (x, y, z) is
+ *     element (z * H + y) * W + x;
+ *   - M is a per-pose 3x4 row-major affine from camera space (mm) to voxel
+ *     index space, so sample s of ray n sits at
+ *         p = M @ [lerp(src_n, tgt_n, t_s), 1],  t_s = s / (n_samples - 1);
+ *   - each sample is a trilinear interpolation with zero padding per corner
+ *     (grid_sample bilinear, align_corners=False in voxel-index form);
+ *   - with n_classes > 1 each sample is routed to the channel given by the
+ *     nearest label (round half to even) at the same position; labels outside
+ *     [0, n_classes) are dropped;
+ *   - out[b, c, n] = step[b, n] * sum of the samples routed to channel c.
+ */
+#ifndef NANODRR_GB300_H
+#define NANODRR_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NDRR_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define NDRR_API __attribute__((visibility("default")))
+#else
+#define NDRR_API
+#endif
+
+/* ---- status codes --------------------------------------------------------- */
+enum ndrr_status {
+    NDRR_OK = 0,
+    NDRR_ERR_INVALID_ARGUMENT = 1, /* bad shape, null pointer, n_samples < 2 ...  */
+    NDRR_ERR_LIMIT = 2,            /* exceeds the int32 indexing or channel limits */
+    NDRR_ERR_DTYPE = 3,            /* unsupported element type                     */
+    NDRR_ERR_WORKSPACE = 4,        /* workspace missing or too small               */
+    NDRR_ERR_CUDA = 5,             /* a CUDA runtime call or launch failed         */
+    NDRR_ERR_DEVICE_TIMEOUT = 6,   /* a bounded device-side wait gave up           */
+};
+
+/* ---- element types -------------------------------------------------------- */
+enum ndrr_dtype {
+    NDRR_F32 = 0,
+    NDRR_F16 = 1,
+    NDRR_BF16 = 2,
+    NDRR_U8 = 3,
+    NDRR_I8 = 4,
+    NDRR_I16 = 5,
+    NDRR_I32 = 6,
+    NDRR_I64 = 7,
+};
+
+/* ---- ray-march arguments --------------------------------------------------- *
+ * One struct serves the forward and the adjoint; fields a call does not use
+ * may be zero/NULL. Pointers are device pointers unless stated otherwise.     */
+typedef struct ndrr_raymarch_args {
+    uint32_t struct_size;   /* sizeof(ndrr_raymarch_args), checked by the library */
+    uint32_t abi_version;   /* NDRR_ABI_VERSION                                   */
+
+    /* Volume [D, H, W], contiguous: f32, f16 or bf16. */
+    const void* vol;
+    int32_t vol_dtype;
+    int32_t D, H, W;
+
+    /* Label map [D, H, W], contiguous, any ndrr_dtype; read only when
+     * n_classes > 1. Float labels are truncated toward zero like a cast. */
+    const void* lab;
+    int32_t lab_dtype;
+    int32_t n_classes;      /* C >= 1 */
+
+    /* Geometry. M: [B, 3, 4] f32. src: [B, 1, 3] (src_per_ray = 0, one source
+     * per pose) or [B, N, 3] (src_per_ray = 1), f32. tgt: [B, N, 3] f32.
+     * step: [B, N] f32 (camera-space sample spacing, mm). All contiguous. */
+    const float* M;
+    const float* src;
+    const float* tgt;
+    const float* step;
+    int32_t src_per_ray;
+    int32_t B;              /* poses                                            */
+    int32_t N;              /* rays per pose                                    */
+    int32_t width;          /* detector width; rays form a (N / width) x width
+                               image when width > 0 and divides N, else a list */
+    int32_t n_samples;      /* samples per ray, >= 2                            */
+
+    /* Optional per-ray sample window [B, N, 2] f32 in units of t (0 = src,
+     * 1 = tgt), or NULL. Samples with t outside [lo, hi] are skipped. Used by
+     * the empty-space proposal; NULL marches the full (box-culled) ray. */
+    const float* t_window;
+
+    /* Forward output [B, C, N], dtype out_dtype (f32, f16 or bf16). When
+     * out_total is non-NULL it receives the unrouted line integral [B, N]
+     * (the single-channel render) in out_dtype as well. */
+    void* out;
+    int32_t out_dtype;
+    void* out_total;
+
+    /* Adjoint inputs/outputs. go: [B, C, N] upstream gradient, dtype go_dtype.
+     * gvol: [D, H, W] f32, ACCUMULATED into (zero it first).
+     * gM: [B, 3, 4] f32, written. gsrc: [B, 1, 3] or [B, N, 3] f32 (following
+     * src_per_ray), gtgt: [B, N, 3] f32 and gstep: [B, N] f32, written when
+     * need_gcam. */
+    const void* go;
+    int32_t go_dtype;
+    int32_t need_gvol;
+    int32_t need_gcam;
+    float* gvol;
+    float* gM;
+    float* gsrc;
+    float* gtgt;
+    float* gstep;
+
+    /* Scratch for the adjoint's deterministic per-tile pose partials. */
+    void* workspace;
+    uint64_t workspace_bytes;
+
+    /* Launch tuning; 0 selects the library default for each. */
+    int32_t tile_w;         /* detector tile width in rays (8 or 16)            */
+    int32_t tile_h;         /* detector tile height in rays (8 or 16)           */
+    int32_t sample_split;   /* 1, 2 or 4 sample chunks per ray within a CTA     */
+    int32_t reserved[5];
+} ndrr_raymarch_args;
+
+/* Library identity. */
+NDRR_API int32_t ndrr_abi_version(void);
+NDRR_API const char* ndrr_build_info(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+NDRR_API const char* ndrr_last_error(void);
+
+/* Forward ray march. Replaces the custom op nanodrr::fused_raymarch
+ * (reference src/nanodrr/drr/_fused.py:415-460): same inputs (vol, lab, M,
+ * src, tgt, step, n_samples, n_classes, width), caller-allocated output. The
+ * split-partials buffer and the final sum/cast of the reference are not
+ * needed: the output is reduced inside each CTA and written in out_dtype. */
+NDRR_API int32_t ndrr_raymarch_fwd(const ndrr_raymarch_args* args, void* stream);
+
+/* Bytes of scratch ndrr_raymarch_bwd needs for `args` (0 is possible). */
+NDRR_API int32_t ndrr_raymarch_bwd_workspace_bytes(const ndrr_raymarch_args* args, uint64_t* bytes);
+
+/* Adjoint ray march. Replaces nanodrr::fused_raymarch_bwd (reference
+ * src/nanodrr/drr/_fused.py:477-531): recomputes the samples, writes the pose
+ * gradient gM deterministically (fixed-order reduction of per-tile partials),
+ * optional camera-space gradients (gsrc summed over rays when src is one per
+ * pose, as the reference's _backward does at _fused.py:552-553) and
+ * accumulates the volume gradient with atomics (not bitwise deterministic). */
+NDRR_API int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* args, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NANODRR_GB300_H */

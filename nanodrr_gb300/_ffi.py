@@ -1,0 +1,139 @@
+"""ctypes binding of the C ABI declared in `include/nanodrr_gb300.h`.
+
+The library is loaded from the package's `_lib/` directory (built in-tree by
+`nanodrr_gb300._build.build`). There is no fallback: if the library is missing
+or fails to load, every render call raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+from . import _build
+
+# ndrr_status
+NDRR_OK = 0
+NDRR_ERR_INVALID_ARGUMENT = 1
+NDRR_ERR_LIMIT = 2
+NDRR_ERR_DTYPE = 3
+NDRR_ERR_WORKSPACE = 4
+NDRR_ERR_CUDA = 5
+NDRR_ERR_DEVICE_TIMEOUT = 6
+
+# ndrr_dtype
+NDRR_F32, NDRR_F16, NDRR_BF16, NDRR_U8, NDRR_I8, NDRR_I16, NDRR_I32, NDRR_I64 = range(8)
+
+ABI_VERSION = 1
+
+_c_float_p = ctypes.POINTER(ctypes.c_float)
+
+
+class RaymarchArgs(ctypes.Structure):
+    """Mirror of `ndrr_raymarch_args` (field order and types must match)."""
+
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("abi_version", ctypes.c_uint32),
+        ("vol", ctypes.c_void_p),
+        ("vol_dtype", ctypes.c_int32),
+        ("D", ctypes.c_int32),
+        ("H", ctypes.c_int32),
+        ("W", ctypes.c_int32),
+        ("lab", ctypes.c_void_p),
+        ("lab_dtype", ctypes.c_int32),
+        ("n_classes", ctypes.c_int32),
+        ("M", ctypes.c_void_p),
+        ("src", ctypes.c_void_p),
+        ("tgt", ctypes.c_void_p),
+        ("step", ctypes.c_void_p),
+        ("src_per_ray", ctypes.c_int32),
+        ("B", ctypes.c_int32),
+        ("N", ctypes.c_int32),
+        ("width", ctypes.c_int32),
+        ("n_samples", ctypes.c_int32),
+        ("t_window", ctypes.c_void_p),
+        ("out", ctypes.c_void_p),
+        ("out_dtype", ctypes.c_int32),
+        ("out_total", ctypes.c_void_p),
+        ("go", ctypes.c_void_p),
+        ("go_dtype", ctypes.c_int32),
+        ("need_gvol", ctypes.c_int32),
+        ("need_gcam", ctypes.c_int32),
+        ("gvol", ctypes.c_void_p),
+        ("gM", ctypes.c_void_p),
+        ("gsrc", ctypes.c_void_p),
+        ("gtgt", ctypes.c_void_p),
+        ("gstep", ctypes.c_void_p),
+        ("workspace", ctypes.c_void_p),
+        ("workspace_bytes", ctypes.c_uint64),
+        ("tile_w", ctypes.c_int32),
+        ("tile_h", ctypes.c_int32),
+        ("sample_split", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 5),
+    ]
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        self.struct_size = ctypes.sizeof(RaymarchArgs)
+        self.abi_version = ABI_VERSION
+
+
+# Every symbol the header declares, with its ctypes signature.
+SIGNATURES: dict[str, tuple] = {
+    "ndrr_abi_version": (ctypes.c_int32, []),
+    "ndrr_build_info": (ctypes.c_char_p, []),
+    "ndrr_last_error": (ctypes.c_char_p, []),
+    "ndrr_raymarch_fwd": (ctypes.c_int32, [ctypes.POINTER(RaymarchArgs), ctypes.c_void_p]),
+    "ndrr_raymarch_bwd_workspace_bytes": (
+        ctypes.c_int32,
+        [ctypes.POINTER(RaymarchArgs), ctypes.POINTER(ctypes.c_uint64)],
+    ),
+    "ndrr_raymarch_bwd": (ctypes.c_int32, [ctypes.POINTER(RaymarchArgs), ctypes.c_void_p]),
+}
+
+_lock = threading.Lock()
+_lib: ctypes.CDLL | None = None
+
+
+def library_path() -> Path:
+    return _build.lib_path()
+
+
+def load(build_if_missing: bool = True) -> ctypes.CDLL:
+    """Load (building first if needed) the shared library and bind signatures."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = library_path()
+        if not path.exists() and build_if_missing:
+            _build.build()
+        if not path.exists():
+            raise RuntimeError(f"nanodrr_gb300 CUDA library not found at {path}; run nanodrr_gb300.build()")
+        lib = ctypes.CDLL(str(path))
+        for name, (restype, argtypes) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = restype
+            fn.argtypes = argtypes
+        ver = lib.ndrr_abi_version()
+        if ver != ABI_VERSION:
+            raise RuntimeError(f"nanodrr_gb300 library ABI {ver} does not match the bindings' {ABI_VERSION}")
+        _lib = lib
+        return lib
+
+
+class NdrrError(RuntimeError):
+    pass
+
+
+def check(rc: int, what: str) -> None:
+    """Map a C-ABI status to the reference's exception types."""
+    if rc == NDRR_OK:
+        return
+    msg = load().ndrr_last_error().decode(errors="replace")
+    text = f"{what}: {msg}"
+    if rc in (NDRR_ERR_INVALID_ARGUMENT, NDRR_ERR_LIMIT, NDRR_ERR_DTYPE):
+        raise ValueError(text)
+    raise NdrrError(text)

@@ -1,0 +1,159 @@
+// extern "C" entry points: argument validation, launch-shape selection and
+// error reporting. Validation mirrors the reference's host-side checks
+// (n_samples >= 2 at nanodrr src/nanodrr/drr/renderer.py:71-72, the int32
+// indexing limits of fused_supported at src/nanodrr/drr/backends.py:66-69)
+// and adds the pointer/dtype/shape checks a C caller needs. Nothing here
+// allocates device memory or synchronises.
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+
+#include "ndrr_launch.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int32_t fail(int32_t code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int32_t ok() {
+    g_last_error.clear();
+    return NDRR_OK;
+}
+
+bool is_float_dtype(int32_t d) { return d == NDRR_F32 || d == NDRR_F16 || d == NDRR_BF16; }
+bool is_any_dtype(int32_t d) { return d >= NDRR_F32 && d <= NDRR_I64; }
+
+constexpr long long kInt32Max = 2147483647LL;
+constexpr int kMaxBlock = 512;
+constexpr size_t kMaxSmem = 227 * 1024;
+
+int sm_count_current() {
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 148;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) return 148;
+    return sms;
+}
+
+// Shape/pointer checks shared by the forward and the adjoint.
+int32_t validate_common(const ndrr_raymarch_args* a) {
+    if (a == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "args is NULL");
+    if (a->struct_size != sizeof(ndrr_raymarch_args))
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "struct_size %u does not match the library's %zu", a->struct_size,
+                    sizeof(ndrr_raymarch_args));
+    if (a->abi_version != NDRR_ABI_VERSION)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "abi_version %u, library is %d", a->abi_version, NDRR_ABI_VERSION);
+    if (a->n_samples < 2) return fail(NDRR_ERR_INVALID_ARGUMENT, "n_samples must be at least 2 (got %d)", a->n_samples);
+    if (a->B < 0 || a->N < 0) return fail(NDRR_ERR_INVALID_ARGUMENT, "negative batch (%d) or ray count (%d)", a->B, a->N);
+    if (a->D < 1 || a->H < 1 || a->W < 1)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "volume dims must be positive (got %d x %d x %d)", a->D, a->H, a->W);
+    if (!is_float_dtype(a->vol_dtype))
+        return fail(NDRR_ERR_DTYPE, "volume dtype %d unsupported (f32, f16, bf16)", a->vol_dtype);
+    if (a->vol == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "vol is NULL");
+    const long long numel = (long long)a->D * a->H * a->W;
+    if (numel >= kInt32Max)
+        return fail(NDRR_ERR_LIMIT, "volume has %lld voxels; the kernels index with int32 (< 2^31)", numel);
+    if (a->n_classes < 1) return fail(NDRR_ERR_INVALID_ARGUMENT, "n_classes must be >= 1 (got %d)", a->n_classes);
+    if (a->n_classes > 1) {
+        if (a->lab == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "n_classes > 1 needs a label map");
+        if (!is_any_dtype(a->lab_dtype)) return fail(NDRR_ERR_DTYPE, "label dtype %d unsupported", a->lab_dtype);
+    }
+    if (a->B == 0 || a->N == 0) return NDRR_OK;
+    if (a->M == nullptr || a->src == nullptr || a->tgt == nullptr || a->step == nullptr)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "M, src, tgt and step must be non-NULL");
+    const long long BN = (long long)a->B * a->N;
+    if ((long long)a->n_classes * BN >= kInt32Max || 3 * BN >= kInt32Max)
+        return fail(NDRR_ERR_LIMIT, "C*B*N = %lld and 3*B*N = %lld must stay below 2^31",
+                    (long long)a->n_classes * BN, 3 * BN);
+    if (a->tile_w != 0 && (a->tile_w % 8 != 0 || a->tile_w < 8 || a->tile_w > 64))
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "tile_w must be a multiple of 8 in [8, 64] (got %d)", a->tile_w);
+    if (a->tile_h != 0 && (a->tile_h % 4 != 0 || a->tile_h < 4 || a->tile_h > 64))
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "tile_h must be a multiple of 4 in [4, 64] (got %d)", a->tile_h);
+    if (a->sample_split != 0 && a->sample_split != 1 && a->sample_split != 2 && a->sample_split != 4)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "sample_split must be 1, 2 or 4 (got %d)", a->sample_split);
+    return NDRR_OK;
+}
+
+int32_t validate_shape(const ndrr::LaunchShape& ls, size_t smem) {
+    const int block = ls.tw * ls.th * ls.K;
+    if (block > kMaxBlock || (block % 32) != 0)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "tile %dx%d with sample_split %d gives %d threads (max %d)", ls.tw,
+                    ls.th, ls.K, block, kMaxBlock);
+    if (smem > kMaxSmem)
+        return fail(NDRR_ERR_LIMIT, "launch needs %zu bytes of shared memory (max %zu); reduce n_classes or the tile",
+                    smem, kMaxSmem);
+    return NDRR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int32_t ndrr_abi_version(void) { return NDRR_ABI_VERSION; }
+
+const char* ndrr_build_info(void) {
+    return "nanodrr_gb300 abi " "1" " sm_103a nvcc " __DATE__;
+}
+
+const char* ndrr_last_error(void) { return g_last_error.c_str(); }
+
+int32_t ndrr_raymarch_fwd(const ndrr_raymarch_args* a, void* stream) {
+    int32_t rc = validate_common(a);
+    if (rc != NDRR_OK) return rc;
+    if (a->B == 0 || a->N == 0) return ok();
+    if (a->out == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "out is NULL");
+    if (!is_float_dtype(a->out_dtype)) return fail(NDRR_ERR_DTYPE, "out dtype %d unsupported", a->out_dtype);
+    const ndrr::LaunchShape ls = ndrr::choose_shape(*a, sm_count_current());
+    rc = validate_shape(ls, ndrr::fwd_smem_bytes(*a, ls));
+    if (rc != NDRR_OK) return rc;
+    const cudaError_t e = ndrr::launch_fwd(*a, ls, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "forward launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
+int32_t ndrr_raymarch_bwd_workspace_bytes(const ndrr_raymarch_args* a, uint64_t* bytes) {
+    if (bytes == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "bytes is NULL");
+    *bytes = 0;
+    int32_t rc = validate_common(a);
+    if (rc != NDRR_OK) return rc;
+    if (a->B == 0 || a->N == 0) return ok();
+    // The partial buffer depends on the tile shape only, not on the sample
+    // split, so no device query is needed (this call never touches the GPU).
+    const ndrr::LaunchShape ls = ndrr::choose_shape(*a, 0);
+    *bytes = ndrr::bwd_workspace_bytes(*a, ls);
+    return ok();
+}
+
+int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* a, void* stream) {
+    int32_t rc = validate_common(a);
+    if (rc != NDRR_OK) return rc;
+    if (a->B == 0 || a->N == 0) return ok();
+    if (a->go == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "go is NULL");
+    if (!is_float_dtype(a->go_dtype)) return fail(NDRR_ERR_DTYPE, "go dtype %d unsupported", a->go_dtype);
+    if (a->gM == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "gM is NULL");
+    if (a->need_gvol && a->gvol == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "need_gvol set but gvol is NULL");
+    if (a->need_gcam && (a->gsrc == nullptr || a->gtgt == nullptr || a->gstep == nullptr))
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "need_gcam set but gsrc/gtgt/gstep is NULL");
+    // Workspace size depends on the tile shape only: check it before any
+    // device query so a bad call fails without touching the GPU.
+    const uint64_t need = ndrr::bwd_workspace_bytes(*a, ndrr::choose_shape(*a, 0));
+    if (a->workspace == nullptr || a->workspace_bytes < need)
+        return fail(NDRR_ERR_WORKSPACE, "adjoint needs %llu workspace bytes, got %llu", (unsigned long long)need,
+                    (unsigned long long)(a->workspace ? a->workspace_bytes : 0));
+    const ndrr::LaunchShape ls = ndrr::choose_shape(*a, sm_count_current());
+    rc = validate_shape(ls, ndrr::bwd_smem_bytes(*a, ls));
+    if (rc != NDRR_OK) return rc;
+    const cudaError_t e = ndrr::launch_bwd(*a, ls, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "adjoint launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
+}  // extern "C"

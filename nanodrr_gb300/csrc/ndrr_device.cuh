@@ -1,0 +1,265 @@
+// Device-side helpers shared by the ray-march kernels: element loads, the
+// per-ray set-up (camera -> voxel line and sample window) and the trilinear
+// sample with zero padding.
+//
+// Sampling semantics follow the reference's fused kernel (nanodrr
+// src/nanodrr/drr/_fused.py:133-228), which in turn reproduces grid_sample
+// (bilinear, zeros padding, align_corners=False) in voxel-index coordinates:
+// sample s of a ray sits at p0 + t_s * d with t_s = s / (S - 1); out-of-range
+// corners read as 0; labels use the nearest voxel with ties to even.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/nanodrr_gb300.h"
+
+namespace ndrr {
+
+// ---------------------------------------------------------------- element I/O
+template <typename T>
+__device__ __forceinline__ float ld_vox(const T* __restrict__ p, int idx);
+
+template <>
+__device__ __forceinline__ float ld_vox<float>(const float* __restrict__ p, int idx) {
+    return __ldg(p + idx);
+}
+template <>
+__device__ __forceinline__ float ld_vox<__half>(const __half* __restrict__ p, int idx) {
+    return __half2float(__ldg(p + idx));
+}
+template <>
+__device__ __forceinline__ float ld_vox<__nv_bfloat16>(const __nv_bfloat16* __restrict__ p, int idx) {
+    return __bfloat162float(__ldg(p + idx));
+}
+
+template <typename T>
+__device__ __forceinline__ void st_out(T* p, size_t idx, float v);
+template <>
+__device__ __forceinline__ void st_out<float>(float* p, size_t idx, float v) { p[idx] = v; }
+template <>
+__device__ __forceinline__ void st_out<__half>(__half* p, size_t idx, float v) { p[idx] = __float2half_rn(v); }
+template <>
+__device__ __forceinline__ void st_out<__nv_bfloat16>(__nv_bfloat16* p, size_t idx, float v) {
+    p[idx] = __float2bfloat16_rn(v);
+}
+
+// Generic element read used for labels and upstream gradients, whose dtype is
+// a runtime value (uniform across the launch, so the switch never diverges).
+__device__ __forceinline__ float ld_any_f(const void* __restrict__ p, int dtype, size_t idx) {
+    switch (dtype) {
+        case NDRR_F32: return __ldg(reinterpret_cast<const float*>(p) + idx);
+        case NDRR_F16: return __half2float(__ldg(reinterpret_cast<const __half*>(p) + idx));
+        case NDRR_BF16: return __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(p) + idx));
+        default: return 0.f;
+    }
+}
+
+// Label value -> class index. Float labels convert with truncation toward zero
+// (a cast, as `.to(int32)` / `.long()` do in the reference, _fused.py:228 and
+// backends.py:57). Values that do not fit in int32 map to -1 (dropped).
+__device__ __forceinline__ int ld_label(const void* __restrict__ p, int dtype, int idx) {
+    switch (dtype) {
+        case NDRR_F32: {
+            float v = __ldg(reinterpret_cast<const float*>(p) + idx);
+            return (v > -2147483520.f && v < 2147483520.f) ? __float2int_rz(v) : -1;
+        }
+        case NDRR_F16: return __float2int_rz(__half2float(__ldg(reinterpret_cast<const __half*>(p) + idx)));
+        case NDRR_BF16: {
+            float v = __bfloat162float(__ldg(reinterpret_cast<const __nv_bfloat16*>(p) + idx));
+            return (v > -2147483520.f && v < 2147483520.f) ? __float2int_rz(v) : -1;
+        }
+        case NDRR_U8: return (int)__ldg(reinterpret_cast<const uint8_t*>(p) + idx);
+        case NDRR_I8: return (int)__ldg(reinterpret_cast<const int8_t*>(p) + idx);
+        case NDRR_I16: return (int)__ldg(reinterpret_cast<const int16_t*>(p) + idx);
+        case NDRR_I32: return __ldg(reinterpret_cast<const int*>(p) + idx);
+        case NDRR_I64: {
+            long long v = __ldg(reinterpret_cast<const long long*>(p) + idx);
+            return (v >= -2147483647LL && v <= 2147483647LL) ? (int)v : -1;
+        }
+        default: return -1;
+    }
+}
+
+// ------------------------------------------------------------------ geometry
+struct Ray {
+    float p0x, p0y, p0z;  // voxel-space position of the source (t = 0)
+    float dx, dy, dz;     // voxel-space displacement src -> tgt
+    int lo, hi;           // sample window [lo, hi): samples outside contribute 0
+};
+
+// Parameter interval where lo <= p + t * d <= hi along one axis.
+__device__ __forceinline__ void axis_interval(float p, float d, float lo, float hi, float& t0, float& t1) {
+    if (fabsf(d) < 1e-20f) {
+        const bool inside = (p >= lo) && (p <= hi);
+        t0 = inside ? -INFINITY : INFINITY;
+        t1 = inside ? INFINITY : -INFINITY;
+        return;
+    }
+    const float inv = 1.0f / d;
+    const float a = (lo - p) * inv;
+    const float b = (hi - p) * inv;
+    t0 = fminf(a, b);
+    t1 = fmaxf(a, b);
+}
+
+// Sample window of a ray: every sample whose trilinear footprint can touch the
+// volume lies in [lo, hi). The box is the footprint support (-1, dim) widened
+// by one voxel, and the index range is widened by -2/+3 samples, so rounding
+// in this set-up can never drop a contributing sample (the same conservative
+// rule as the reference's cull, _fused.py:144-155, applied per ray instead of
+// per 128-ray program). Skipped samples contribute exactly zero to every
+// output and gradient.
+__device__ __forceinline__ void ray_window(Ray& r, int D, int H, int W, int S) {
+    float ax0, ax1, ay0, ay1, az0, az1;
+    axis_interval(r.p0x, r.dx, -2.0f, (float)W + 1.0f, ax0, ax1);
+    axis_interval(r.p0y, r.dy, -2.0f, (float)H + 1.0f, ay0, ay1);
+    axis_interval(r.p0z, r.dz, -2.0f, (float)D + 1.0f, az0, az1);
+    const float t_lo = fmaxf(fmaxf(ax0, ay0), az0);
+    const float t_hi = fminf(fminf(ax1, ay1), az1);
+    const float sm1 = (float)(S - 1);
+    if (!(t_lo <= t_hi)) {
+        r.lo = 0;
+        r.hi = 0;
+        return;
+    }
+    // Clamp before converting so huge or infinite parameters stay in range.
+    const float f_lo = fminf(fmaxf(floorf(t_lo * sm1) - 2.0f, 0.0f), (float)S);
+    const float f_hi = fminf(fmaxf(ceilf(t_hi * sm1) + 3.0f, 0.0f), (float)S);
+    r.lo = (int)f_lo;
+    r.hi = (int)f_hi;
+}
+
+// Intersect the window with an optional per-ray [t_lo, t_hi] (in units of t).
+__device__ __forceinline__ void apply_t_window(Ray& r, float wlo, float whi, int S) {
+    const float sm1 = (float)(S - 1);
+    const float a = fminf(fmaxf(ceilf(wlo * sm1), 0.0f), (float)S);
+    const float b = fminf(fmaxf(floorf(whi * sm1) + 1.0f, 0.0f), (float)S);
+    r.lo = max(r.lo, (int)a);
+    r.hi = min(r.hi, (int)b);
+}
+
+// ------------------------------------------------------------ trilinear tap
+// The eight corners of the cell containing (x, y, z), zero outside the volume,
+// and the fractional offsets inside the cell.
+struct Cell {
+    float v000, v001, v010, v011, v100, v101, v110, v111;  // v[z][y][x] offsets
+    float fx, fy, fz;
+    int ix, iy, iz;
+};
+
+template <typename VT>
+__device__ __forceinline__ void load_cell(const VT* __restrict__ vol, int D, int H, int W, float x, float y,
+                                          float z, Cell& c) {
+    // Positions are clamped to [-2, dim + 1] first: beyond that every corner
+    // is outside the volume either way, and the clamp keeps the float -> int
+    // conversion in range for any input.
+    x = fminf(fmaxf(x, -2.0f), (float)W + 1.0f);
+    y = fminf(fmaxf(y, -2.0f), (float)H + 1.0f);
+    z = fminf(fmaxf(z, -2.0f), (float)D + 1.0f);
+    const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+    c.fx = x - xf;
+    c.fy = y - yf;
+    c.fz = z - zf;
+    const int ix = (int)xf, iy = (int)yf, iz = (int)zf;
+    c.ix = ix;
+    c.iy = iy;
+    c.iz = iz;
+    const int HW = H * W;
+    const int base = (iz * H + iy) * W + ix;
+    if ((unsigned)ix < (unsigned)(W - 1) && (unsigned)iy < (unsigned)(H - 1) && (unsigned)iz < (unsigned)(D - 1)) {
+        c.v000 = ld_vox(vol, base);
+        c.v001 = ld_vox(vol, base + 1);
+        c.v010 = ld_vox(vol, base + W);
+        c.v011 = ld_vox(vol, base + W + 1);
+        c.v100 = ld_vox(vol, base + HW);
+        c.v101 = ld_vox(vol, base + HW + 1);
+        c.v110 = ld_vox(vol, base + HW + W);
+        c.v111 = ld_vox(vol, base + HW + W + 1);
+    } else {
+        const bool x0 = (unsigned)ix < (unsigned)W, x1 = (unsigned)(ix + 1) < (unsigned)W;
+        const bool y0 = (unsigned)iy < (unsigned)H, y1 = (unsigned)(iy + 1) < (unsigned)H;
+        const bool z0 = (unsigned)iz < (unsigned)D, z1 = (unsigned)(iz + 1) < (unsigned)D;
+        c.v000 = (z0 && y0 && x0) ? ld_vox(vol, base) : 0.f;
+        c.v001 = (z0 && y0 && x1) ? ld_vox(vol, base + 1) : 0.f;
+        c.v010 = (z0 && y1 && x0) ? ld_vox(vol, base + W) : 0.f;
+        c.v011 = (z0 && y1 && x1) ? ld_vox(vol, base + W + 1) : 0.f;
+        c.v100 = (z1 && y0 && x0) ? ld_vox(vol, base + HW) : 0.f;
+        c.v101 = (z1 && y0 && x1) ? ld_vox(vol, base + HW + 1) : 0.f;
+        c.v110 = (z1 && y1 && x0) ? ld_vox(vol, base + HW + W) : 0.f;
+        c.v111 = (z1 && y1 && x1) ? ld_vox(vol, base + HW + W + 1) : 0.f;
+    }
+}
+
+__device__ __forceinline__ float cell_value(const Cell& c) {
+    const float c00 = fmaf(c.fx, c.v001 - c.v000, c.v000);
+    const float c01 = fmaf(c.fx, c.v011 - c.v010, c.v010);
+    const float c10 = fmaf(c.fx, c.v101 - c.v100, c.v100);
+    const float c11 = fmaf(c.fx, c.v111 - c.v110, c.v110);
+    const float c0 = fmaf(c.fy, c01 - c00, c00);
+    const float c1 = fmaf(c.fy, c11 - c10, c10);
+    return fmaf(c.fz, c1 - c0, c0);
+}
+
+// Analytic derivative of the trilinear interpolant with respect to the
+// voxel-space position (the partial derivatives of the formula above).
+__device__ __forceinline__ void cell_grad(const Cell& c, float& gx, float& gy, float& gz) {
+    const float wx0 = 1.f - c.fx, wy0 = 1.f - c.fy, wz0 = 1.f - c.fz;
+    gx = ((c.v001 - c.v000) * wy0 + (c.v011 - c.v010) * c.fy) * wz0 +
+         ((c.v101 - c.v100) * wy0 + (c.v111 - c.v110) * c.fy) * c.fz;
+    gy = ((c.v010 - c.v000) * wx0 + (c.v011 - c.v001) * c.fx) * wz0 +
+         ((c.v110 - c.v100) * wx0 + (c.v111 - c.v101) * c.fx) * c.fz;
+    gz = ((c.v100 - c.v000) * wx0 + (c.v101 - c.v001) * c.fx) * wy0 +
+         ((c.v110 - c.v010) * wx0 + (c.v111 - c.v011) * c.fx) * c.fy;
+}
+
+// Nearest-voxel label at (x, y, z); ties round to even like grid_sample's
+// nearest mode. Out-of-volume positions read label 0 (zero padding).
+__device__ __forceinline__ int nearest_label(const void* __restrict__ lab, int lab_dtype, int D, int H, int W,
+                                             float x, float y, float z) {
+    x = fminf(fmaxf(x, -2.0f), (float)W + 1.0f);
+    y = fminf(fmaxf(y, -2.0f), (float)H + 1.0f);
+    z = fminf(fmaxf(z, -2.0f), (float)D + 1.0f);
+    const int rx = (int)rintf(x), ry = (int)rintf(y), rz = (int)rintf(z);
+    if ((unsigned)rx < (unsigned)W && (unsigned)ry < (unsigned)H && (unsigned)rz < (unsigned)D)
+        return ld_label(lab, lab_dtype, (rz * H + ry) * W + rx);
+    return 0;
+}
+
+// --------------------------------------------------------------- tile layout
+// A CTA owns a tile_w x tile_h patch of detector pixels; each warp owns an
+// 8 x 4 sub-patch so that the 32 lanes of a gather hit a compact footprint
+// in the plane across the rays.
+struct TileMap {
+    int IW, IH;      // image (or virtual image) extent in rays
+    int tiles_x;     // tiles per image row
+    int tiles;       // tiles per pose
+    bool linear;     // rays are a flat list (virtual width 16)
+};
+
+__host__ __device__ __forceinline__ TileMap make_tilemap(int N, int width, int tw, int th) {
+    TileMap m;
+    m.linear = !(width > 0 && N % width == 0);
+    m.IW = m.linear ? 16 : width;
+    m.IH = m.linear ? (N + 15) / 16 : N / width;
+    m.tiles_x = (m.IW + tw - 1) / tw;
+    m.tiles = m.tiles_x * ((m.IH + th - 1) / th);
+    return m;
+}
+
+// Ray index of lane `r` (0 <= r < tw * th) of tile `tile`, or -1 if padding.
+// tw is a multiple of 8 and th a multiple of 4.
+__device__ __forceinline__ int tile_ray(const TileMap& m, int N, int tw, int th, int tile, int r) {
+    const int warp = r >> 5, lane = r & 31;
+    const int wpr = tw >> 3;  // warps per tile row
+    const int tx = tile % m.tiles_x, ty = tile / m.tiles_x;
+    const int px = tx * tw + (warp % wpr) * 8 + (lane & 7);
+    const int py = ty * th + (warp / wpr) * 4 + (lane >> 3);
+    if (px >= m.IW || py >= m.IH) return -1;
+    const int n = py * m.IW + px;
+    return n < N ? n : -1;
+}
+
+}  // namespace ndrr

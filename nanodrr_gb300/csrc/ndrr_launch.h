@@ -1,0 +1,25 @@
+// Internal launch interface between the C ABI (ndrr_capi.cu) and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/nanodrr_gb300.h"
+
+namespace ndrr {
+
+struct LaunchShape {
+    int tw = 16;  // tile width in rays (multiple of 8)
+    int th = 8;   // tile height in rays (multiple of 4)
+    int K = 1;    // sample chunks per ray within a CTA
+};
+
+LaunchShape choose_shape(const ndrr_raymarch_args& a, int sm_count);
+uint64_t bwd_workspace_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
+size_t fwd_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
+size_t bwd_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
+
+cudaError_t launch_fwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
+cudaError_t launch_bwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
+
+}  // namespace ndrr

@@ -1,0 +1,309 @@
+"""Torch custom ops over the C ABI: `nanodrr_gb300::fused_raymarch` and
+`nanodrr_gb300::fused_raymarch_bwd`.
+
+Same schemas and argument meaning as the reference's ops
+`nanodrr::fused_raymarch` (nanodrr src/nanodrr/drr/_fused.py:415-426) and
+`nanodrr::fused_raymarch_bwd` (_fused.py:477-491), registered with fake
+(meta) kernels for `torch.compile` (_fused.py:463, 534) and an autograd
+formula (_fused.py:545-567). The work happens in `libnanodrr_gb300.so`; this
+module only allocates outputs with the torch caching allocator, passes raw
+pointers and the current stream, and maps C-ABI status codes to exceptions.
+
+Differences from the reference, by design:
+  - the forward writes its output in `vol.dtype` directly (no split-partials
+    buffer and no separate sum/cast pass);
+  - the backward returns `gsrc` already shaped like `src` (the reference's op
+    returns per-ray `[B, N, 3]` and its autograd glue sums over rays when the
+    source is shared, _fused.py:552-553; here that sum happens in-kernel).
+"""
+
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from . import _ffi
+
+_TORCH_TO_NDRR = {
+    torch.float32: _ffi.NDRR_F32,
+    torch.float16: _ffi.NDRR_F16,
+    torch.bfloat16: _ffi.NDRR_BF16,
+    torch.uint8: _ffi.NDRR_U8,
+    torch.bool: _ffi.NDRR_U8,
+    torch.int8: _ffi.NDRR_I8,
+    torch.int16: _ffi.NDRR_I16,
+    torch.int32: _ffi.NDRR_I32,
+    torch.int64: _ffi.NDRR_I64,
+}
+_FLOAT_DTYPES = (torch.float32, torch.float16, torch.bfloat16)
+
+
+def ndrr_dtype(t: torch.Tensor) -> int:
+    try:
+        return _TORCH_TO_NDRR[t.dtype]
+    except KeyError:
+        raise ValueError(f"unsupported dtype {t.dtype}") from None
+
+
+def _stream_handle(device: torch.device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def _ptr(t: torch.Tensor | None) -> int | None:
+    if t is None or t.numel() == 0:
+        return None
+    return t.data_ptr()
+
+
+def _check_inputs(vol, lab, M, src, tgt, step, n_samples, n_classes):
+    if not vol.is_cuda:
+        raise RuntimeError("nanodrr_gb300 renders on CUDA devices only (got a volume on %s)" % vol.device)
+    if vol.dim() != 3:
+        raise ValueError(f"vol must be [D, H, W], got shape {tuple(vol.shape)}")
+    if vol.dtype not in _FLOAT_DTYPES:
+        raise ValueError(f"vol dtype {vol.dtype} unsupported; use float32, float16 or bfloat16")
+    if n_samples < 2:
+        raise ValueError("n_samples must be at least 2")
+    if tgt.dim() != 3 or tgt.shape[-1] != 3:
+        raise ValueError(f"tgt must be [B, N, 3], got {tuple(tgt.shape)}")
+    B, N, _ = tgt.shape
+    if M.shape != (B, 3, 4):
+        raise ValueError(f"M must be [B, 3, 4] = [{B}, 3, 4], got {tuple(M.shape)}")
+    if src.dim() != 3 or src.shape[0] != B or src.shape[1] not in (1, N) or src.shape[2] != 3:
+        raise ValueError(f"src must be [B, 1, 3] or [B, N, 3], got {tuple(src.shape)}")
+    if step.shape != (B, N):
+        raise ValueError(f"step must be [B, N] = [{B}, {N}], got {tuple(step.shape)}")
+    if n_classes > 1 and lab.shape != vol.shape:
+        raise ValueError(f"label map shape {tuple(lab.shape)} does not match the volume {tuple(vol.shape)}")
+    for name, t in (("lab", lab), ("M", M), ("src", src), ("tgt", tgt), ("step", step)):
+        if t.device != vol.device:
+            raise ValueError(f"{name} is on {t.device}, the volume on {vol.device}")
+
+
+def _base_args(vol, lab, M, src, tgt, step, n_samples, n_classes, width) -> _ffi.RaymarchArgs:
+    B, N, _ = tgt.shape
+    D, H, W = vol.shape
+    a = _ffi.RaymarchArgs()
+    a.vol = vol.data_ptr()
+    a.vol_dtype = ndrr_dtype(vol)
+    a.D, a.H, a.W = D, H, W
+    a.n_classes = n_classes
+    if n_classes > 1:
+        a.lab = lab.data_ptr()
+        a.lab_dtype = ndrr_dtype(lab)
+    a.M = _ptr(M)
+    a.src = _ptr(src)
+    a.tgt = _ptr(tgt)
+    a.step = _ptr(step)
+    a.src_per_ray = 0 if src.shape[1] == 1 else 1
+    a.B, a.N = B, N
+    a.width = width
+    a.n_samples = n_samples
+    return a
+
+
+def _prep(vol, lab, M, src, tgt, step):
+    vol = vol.contiguous()
+    lab = lab.contiguous()
+    M = M.float().contiguous()
+    src = src.float().contiguous()
+    tgt = tgt.float().contiguous()
+    step = step.float().contiguous()
+    return vol, lab, M, src, tgt, step
+
+
+def raymarch_forward(
+    vol: torch.Tensor,
+    lab: torch.Tensor,
+    M: torch.Tensor,
+    src: torch.Tensor,
+    tgt: torch.Tensor,
+    step: torch.Tensor,
+    n_samples: int,
+    n_classes: int,
+    width: int,
+    t_window: torch.Tensor | None = None,
+    with_total: bool = False,
+    out_dtype: torch.dtype | None = None,
+) -> tuple[torch.Tensor, torch.Tensor | None]:
+    """Launch the forward kernel; returns (out [B, C, N], total [B, N] or None)."""
+    _check_inputs(vol, lab, M, src, tgt, step, n_samples, n_classes)
+    vol, lab, M, src, tgt, step = _prep(vol, lab, M, src, tgt, step)
+    B, N, _ = tgt.shape
+    odt = out_dtype or vol.dtype
+    out = torch.empty(B, n_classes, N, device=vol.device, dtype=odt)
+    total = torch.empty(B, N, device=vol.device, dtype=odt) if with_total else None
+    a = _base_args(vol, lab, M, src, tgt, step, n_samples, n_classes, width)
+    a.out = _ptr(out)
+    a.out_dtype = ndrr_dtype(out)
+    a.out_total = _ptr(total)
+    if t_window is not None:
+        t_window = t_window.float().contiguous()
+        if t_window.shape != (B, N, 2):
+            raise ValueError(f"t_window must be [B, N, 2], got {tuple(t_window.shape)}")
+        a.t_window = _ptr(t_window)
+    lib = _ffi.load()
+    _ffi.check(lib.ndrr_raymarch_fwd(ctypes.byref(a), _stream_handle(vol.device)), "ndrr_raymarch_fwd")
+    return out, total
+
+
+def raymarch_backward(
+    go: torch.Tensor,
+    vol: torch.Tensor,
+    lab: torch.Tensor,
+    M: torch.Tensor,
+    src: torch.Tensor,
+    tgt: torch.Tensor,
+    step: torch.Tensor,
+    n_samples: int,
+    n_classes: int,
+    width: int,
+    need_gvol: bool,
+    need_gcam: bool,
+    t_window: torch.Tensor | None = None,
+    gvol: torch.Tensor | None = None,
+):
+    """Launch the adjoint; returns (gvol, gM, gsrc, gtgt, gstep) in float32.
+
+    `gvol`, when given, is a float32 [D, H, W] buffer the volume gradient is
+    accumulated into (so several calls can share one); otherwise a zeroed one
+    is allocated."""
+    _check_inputs(vol, lab, M, src, tgt, step, n_samples, n_classes)
+    vol, lab, M, src, tgt, step = _prep(vol, lab, M, src, tgt, step)
+    B, N, _ = tgt.shape
+    dev = vol.device
+    go = go.contiguous()
+    if go.shape != (B, n_classes, N):
+        raise ValueError(f"go must be [B, C, N] = [{B}, {n_classes}, {N}], got {tuple(go.shape)}")
+    if go.dtype not in _FLOAT_DTYPES:
+        go = go.float()
+    empty = torch.empty(0, device=dev, dtype=torch.float32)
+    gM = torch.empty(B, 3, 4, device=dev, dtype=torch.float32)
+    if need_gvol:
+        if gvol is None:
+            gvol = torch.zeros(vol.shape, device=dev, dtype=torch.float32)
+        elif gvol.shape != vol.shape or gvol.dtype != torch.float32 or not gvol.is_contiguous():
+            raise ValueError("gvol must be a contiguous float32 tensor shaped like the volume")
+    else:
+        gvol = empty
+    if need_gcam:
+        gsrc = torch.empty(src.shape, device=dev, dtype=torch.float32)
+        gtgt = torch.empty(B, N, 3, device=dev, dtype=torch.float32)
+        gstep = torch.empty(B, N, device=dev, dtype=torch.float32)
+    else:
+        gsrc = gtgt = gstep = empty
+    a = _base_args(vol, lab, M, src, tgt, step, n_samples, n_classes, width)
+    a.go = _ptr(go)
+    a.go_dtype = ndrr_dtype(go)
+    a.need_gvol = int(need_gvol)
+    a.need_gcam = int(need_gcam)
+    a.gvol = _ptr(gvol) if need_gvol else None
+    a.gM = _ptr(gM)
+    if need_gcam:
+        a.gsrc, a.gtgt, a.gstep = _ptr(gsrc), _ptr(gtgt), _ptr(gstep)
+    if t_window is not None:
+        t_window = t_window.float().contiguous()
+        a.t_window = _ptr(t_window)
+    lib = _ffi.load()
+    nbytes = ctypes.c_uint64(0)
+    _ffi.check(lib.ndrr_raymarch_bwd_workspace_bytes(ctypes.byref(a), ctypes.byref(nbytes)), "workspace query")
+    ws = torch.empty(max(int(nbytes.value), 16), device=dev, dtype=torch.uint8)
+    a.workspace = ws.data_ptr()
+    a.workspace_bytes = ws.numel()
+    _ffi.check(lib.ndrr_raymarch_bwd(ctypes.byref(a), _stream_handle(dev)), "ndrr_raymarch_bwd")
+    return gvol, gM, gsrc, gtgt, gstep
+
+
+# --------------------------------------------------------------- custom ops
+@torch.library.custom_op("nanodrr_gb300::fused_raymarch", mutates_args=())
+def fused_raymarch(
+    vol: torch.Tensor,
+    lab: torch.Tensor,
+    M: torch.Tensor,
+    src: torch.Tensor,
+    tgt: torch.Tensor,
+    step: torch.Tensor,
+    n_samples: int,
+    n_classes: int,
+    width: int,
+) -> torch.Tensor:
+    """Differentiable ray march: [B, C, N] line integrals in `vol.dtype`."""
+    out, _ = raymarch_forward(vol, lab, M, src, tgt, step, n_samples, n_classes, width)
+    return out
+
+
+@fused_raymarch.register_fake
+def _(vol, lab, M, src, tgt, step, n_samples, n_classes, width):
+    B, N, _ = tgt.shape
+    return torch.empty(B, n_classes, N, device=vol.device, dtype=vol.dtype)
+
+
+@torch.library.custom_op("nanodrr_gb300::fused_raymarch_bwd", mutates_args=())
+def fused_raymarch_bwd(
+    go: torch.Tensor,
+    vol: torch.Tensor,
+    lab: torch.Tensor,
+    M: torch.Tensor,
+    src: torch.Tensor,
+    tgt: torch.Tensor,
+    step: torch.Tensor,
+    n_samples: int,
+    n_classes: int,
+    width: int,
+    need_gvol: bool,
+    need_gcam: bool,
+) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor]:
+    """Adjoint launch; volume gradients use atomics (reference _fused.py:493-497)."""
+    if need_gvol and torch.are_deterministic_algorithms_enabled():
+        raise RuntimeError(
+            "Volume gradients on the cuda backend use nondeterministic atomics; "
+            "disable deterministic algorithms or detach the volume"
+        )
+    gvol, gM, gsrc, gtgt, gstep = raymarch_backward(
+        go, vol, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam
+    )
+    return gvol, gM, gsrc, gtgt, gstep
+
+
+@fused_raymarch_bwd.register_fake
+def _(go, vol, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam):
+    B, N, _ = tgt.shape
+    gM = torch.empty(B, 3, 4, device=M.device, dtype=torch.float32)
+    empty = gM.new_empty(0)
+    gvol = torch.empty(vol.shape, device=M.device, dtype=torch.float32) if need_gvol else empty
+    gsrc = torch.empty(src.shape, device=M.device, dtype=torch.float32) if need_gcam else empty
+    gtgt = torch.empty(B, N, 3, device=M.device, dtype=torch.float32) if need_gcam else empty
+    gstep = torch.empty(B, N, device=M.device, dtype=torch.float32) if need_gcam else empty
+    return gvol, gM, gsrc, gtgt, gstep
+
+
+def _setup_context(ctx, inputs, output):
+    vol, lab, M, src, tgt, step, n_samples, n_classes, width = inputs
+    ctx.save_for_backward(vol, lab, M.contiguous(), src, tgt, step)
+    ctx.n_samples = n_samples
+    ctx.n_classes = n_classes
+    ctx.width = width
+
+
+def _backward(ctx, go):
+    vol, lab, M, src, tgt, step = ctx.saved_tensors
+    need_gvol = ctx.needs_input_grad[0]
+    need_gcam = any(ctx.needs_input_grad[i] for i in (3, 4, 5))
+    gvol, gM, gsrc, gtgt, gstep = fused_raymarch_bwd(
+        go, vol, lab, M, src, tgt, step, ctx.n_samples, ctx.n_classes, ctx.width, need_gvol, need_gcam
+    )
+    return (
+        gvol.to(vol.dtype) if need_gvol else None,
+        None,  # lab: nearest-label lookup, not differentiable
+        gM.to(M.dtype),
+        gsrc.to(src.dtype) if need_gcam else None,
+        gtgt.to(tgt.dtype) if need_gcam else None,
+        gstep.to(step.dtype) if need_gcam else None,
+        None,
+        None,
+        None,
+    )
+
+
+torch.library.register_autograd("nanodrr_gb300::fused_raymarch", _backward, setup_context=_setup_context)

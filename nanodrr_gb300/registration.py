@@ -1,0 +1,82 @@
+"""Registration step around `render`: pose perturbation and NCC loss.
+
+`Registration` mirrors the reference's module (nanodrr
+src/nanodrr/registration/registration.py:9-84): the optimisable so(3)
+rotation vector and translation perturb the initial pose about the
+volume's isocenter, pose = rt_inv @ pivot @ T(rot, xyz) @ pivot^-1.
+`NormalizedCrossCorrelation2d` mirrors src/nanodrr/metrics/ncc.py:8-37
+(per-image zero-mean, unit-variance correlation, optional patches).
+Both are host-side torch: the heavy part of a registration step is the
+render and its adjoint, which run in the CUDA kernels.
+"""
+
+from __future__ import annotations
+
+import torch
+
+from .geometry import convert, transform_point
+from .renderer import render
+
+
+class Registration(torch.nn.Module):
+    def __init__(self, subject, rt_inv, k_inv, sdd, height, width, eps: float = 1e-8, batch: int | None = None):
+        super().__init__()
+        self.subject = subject
+        self.register_buffer("rt_inv", rt_inv)
+        self.register_buffer("k_inv", k_inv)
+        self.register_buffer("sdd", sdd)
+        self.height = height
+        self.width = width
+        c = transform_point(rt_inv.inverse(), subject.isocenter[None].expand(rt_inv.shape[0], 3)[:, None])[:, 0]
+        self.register_buffer("pivot", self._make_translation(c))
+        self.register_buffer("pivot_inv", self._make_translation(-c))
+        nb = batch if batch is not None else 1
+        self._rot = torch.nn.Parameter(eps * torch.randn(nb, 3, device=c.device))
+        self._xyz = torch.nn.Parameter(eps * torch.randn(nb, 3, device=c.device))
+
+    @property
+    def pose(self) -> torch.Tensor:
+        T = convert(self._rot, self._xyz, "so3_log")
+        return self.rt_inv @ self.pivot @ T @ self.pivot_inv
+
+    def forward(self, n_samples: int = 500, backend: str = "auto") -> torch.Tensor:
+        return render(self.subject, self.k_inv, self.pose, self.sdd, self.height, self.width, n_samples,
+                      backend=backend)
+
+    @staticmethod
+    def _make_translation(t: torch.Tensor) -> torch.Tensor:
+        T = torch.eye(4, device=t.device, dtype=t.dtype)[None].repeat(len(t), 1, 1)
+        T[:, :3, 3] = t
+        return T
+
+
+class NormalizedCrossCorrelation2d(torch.nn.Module):
+    """Score in [-1, 1] per image pair: mean of the product of the two images
+    after each is normalised to zero mean and unit variance (+eps)."""
+
+    def __init__(self, patch_size: int | None = None, eps: float = 1e-7):
+        super().__init__()
+        self.patch_size = patch_size
+        self.eps = eps
+
+    def forward(self, x1: torch.Tensor, x2: torch.Tensor) -> torch.Tensor:
+        if self.patch_size is not None:
+            x1, x2 = _to_patches(x1, self.patch_size), _to_patches(x2, self.patch_size)
+        if x1.shape != x2.shape:
+            raise ValueError("Input images must be the same size")
+        _, c, h, w = x1.shape
+        return (self._norm(x1) * self._norm(x2)).sum(dim=(1, 2, 3)) / (c * h * w)
+
+    def _norm(self, x):
+        mu = x.mean(dim=(-1, -2), keepdim=True)
+        var = x.var(dim=(-1, -2), keepdim=True, correction=0) + self.eps
+        return (x - mu) / var.sqrt()
+
+
+def _to_patches(x: torch.Tensor, p: int) -> torch.Tensor:
+    """[B, C, H, W] -> [B, C * H' * W', p, p]: every p x p window becomes a
+    channel, so the normalisation runs within each window (local NCC), the
+    layout the reference produces at ncc.py:65-74."""
+    x = x.unfold(2, p, step=1).unfold(3, p, step=1).contiguous()
+    b, c, h, w, p1, p2 = x.shape
+    return x.reshape(b, c * h * w, p1, p2)

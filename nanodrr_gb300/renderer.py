@@ -1,0 +1,129 @@
+"""`render`: the user-facing call, a drop-in for the reference's fused backend.
+
+Mirrors nanodrr's `render` (src/nanodrr/drr/renderer.py:21-98) and the
+adapter `render_fused` (src/nanodrr/drr/backends.py:72-117): same arguments,
+same ray construction (`_make_tgt`/`_make_src`, renderer.py:101-132), same
+camera-space step size (renderer.py:82) and the same camera -> voxel affine
+`M = (world_to_voxel @ rt_inv)[:, :3]` in float32 (backends.py:96). There is
+one backend, the sm_103a CUDA kernels: `backend` accepts "auto", "cuda" and
+"triton" (the reference's name for its fused backend, kept so existing calls
+switch unchanged); any other value raises, and CPU tensors raise rather than
+falling back to a CPU path.
+"""
+
+from __future__ import annotations
+
+import torch
+
+from .raymarch import fused_raymarch
+from .subject import Subject
+
+_BACKENDS = ("auto", "cuda", "triton")
+
+
+def fused_supported(subject: Subject, B: int, n_pixels: int) -> bool:
+    """Limits of the CUDA kernels: one volume, int32 voxel and ray indexing
+    (reference backends.py:66-69)."""
+    N = B * n_pixels
+    return subject.image.shape[0] == 1 and max(subject.image.numel(), subject.n_classes * N, 3 * N) < 2**31
+
+
+def _make_tgt(k_inv, sdd, height, width, device, dtype) -> torch.Tensor:
+    """Detector pixel centres (u + 0.5, v + 0.5, 1) mapped by sdd * K^-1."""
+    N = height * width
+    v, u = torch.meshgrid(
+        torch.arange(height, device=device, dtype=dtype) + 0.5,
+        torch.arange(width, device=device, dtype=dtype) + 0.5,
+        indexing="ij",
+    )
+    uv1 = torch.stack([u, v, torch.ones_like(u)], dim=-1).reshape(N, 3)
+    return sdd[:, None, None] * torch.einsum("bij,nj->bni", k_inv, uv1)
+
+
+def _make_src(orthographic: bool, tgt: torch.Tensor, sdd: torch.Tensor) -> torch.Tensor:
+    """Point source at the camera origin, or parallel rays for orthographic."""
+    if orthographic:
+        src = tgt.clone()
+        src[..., 2] -= sdd[:, None]
+        return src
+    B = tgt.shape[0]
+    return torch.zeros(B, 1, 3, device=tgt.device, dtype=tgt.dtype)
+
+
+def compact_label(subject: Subject) -> torch.Tensor:
+    """Label map for the kernels: float labels with n_classes <= 255 are packed
+    to uint8 once per label tensor version (trunc(label) if it is a class in
+    [0, C), else 255, which the kernels drop), saving 3 of 4 bytes per label
+    read with identical routing. Other label maps pass through unchanged."""
+    lab = subject.label[0, 0]
+    C = subject.n_classes
+    if not lab.is_floating_point() or C > 255:
+        return lab.contiguous()
+    key = (lab.data_ptr(), lab._version, lab.dtype, tuple(lab.shape), C, lab.device)
+    cache = getattr(subject, "_ndrr_label_cache", None)
+    if cache is not None and cache[0] == key:
+        return cache[1]
+    t = torch.trunc(lab.float())
+    packed = torch.where((t >= 0) & (t < C), t, torch.full_like(t, 255.0)).to(torch.uint8).contiguous()
+    object.__setattr__(subject, "_ndrr_label_cache", (key, packed))
+    return packed
+
+
+def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) -> torch.Tensor:
+    """Adapter from the render call to the `nanodrr_gb300::fused_raymarch` op."""
+    C = subject.n_classes
+    vol = subject.image[0, 0].contiguous()
+    lab = compact_label(subject) if C > 1 else vol
+    M = (subject.world_to_voxel.float() @ rt_inv.float())[:, :3, :]
+    B = max(M.shape[0], tgt.shape[0])
+    if M.shape[0] != B:
+        M = M.expand(B, -1, -1)
+    if not fused_supported(subject, B, height * width):
+        raise ValueError("inputs exceed the CUDA kernel's limits (int32 indexing)")
+    out = fused_raymarch(
+        vol,
+        lab,
+        M.contiguous(),
+        src.expand(B, -1, -1).float().contiguous(),
+        tgt.expand(B, -1, -1).float().contiguous(),
+        step_size.expand(B, -1).float().contiguous(),
+        n_samples,
+        C,
+        width,
+    )
+    return out.reshape(B, C, height, width)
+
+
+def render(
+    subject: Subject,
+    k_inv: torch.Tensor,
+    rt_inv: torch.Tensor,
+    sdd: torch.Tensor,
+    height: int,
+    width: int,
+    n_samples: int = 500,
+    orthographic: bool = False,
+    src: torch.Tensor | None = None,
+    tgt: torch.Tensor | None = None,
+    backend: str = "auto",
+) -> torch.Tensor:
+    """Differentiable DRR: [B, C, H, W] line integrals of `subject.image`
+    (per label channel when the subject has a multi-class label map).
+
+    Args mirror the reference: `k_inv` [B|1, 3, 3], `rt_inv` [B, 4, 4]
+    (camera -> world), `sdd` [B|1]; optional precomputed camera-space ray
+    endpoints `src` [B, 1|N, 3] and `tgt` [B, N, 3]. Gradients flow to the
+    pose, the intrinsics, the ray endpoints and the volume."""
+    if n_samples < 2:
+        raise ValueError("n_samples must be at least 2")
+    if backend not in _BACKENDS:
+        raise ValueError(f"Unknown backend {backend!r}; expected 'auto', 'cuda', or 'triton'")
+    if not rt_inv.is_cuda or not subject.image.is_cuda:
+        raise RuntimeError("nanodrr_gb300 renders on CUDA devices only; move the subject and poses to a GPU")
+    device, dtype = rt_inv.device, rt_inv.dtype
+    if tgt is None:
+        tgt = _make_tgt(k_inv, sdd, height, width, device, dtype)
+    if src is None:
+        src = _make_src(orthographic, tgt, sdd)
+    step_size = (tgt - src).norm(dim=-1) / float(n_samples - 1)
+    return render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width)

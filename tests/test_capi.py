@@ -1,0 +1,133 @@
+"""The C-ABI library builds, loads and exports every symbol its header declares,
+and its host-side validation rejects bad arguments with the documented status
+codes — all without a GPU (no call here launches a kernel)."""
+
+import ctypes
+import re
+from pathlib import Path
+
+import pytest
+
+from nanodrr_gb300 import _build, _ffi
+
+HEADERS = sorted((Path(__file__).resolve().parents[1] / "include").glob("*.h"))
+
+
+def declared_symbols() -> set[str]:
+    names = set()
+    for h in HEADERS:
+        for m in re.finditer(r"NDRR_API\s+[\w\s\*]+?\b(ndrr_\w+)\s*\(", h.read_text()):
+            names.add(m.group(1))
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    _build.build()
+    return _ffi.load()
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    assert {"ndrr_raymarch_fwd", "ndrr_raymarch_bwd", "ndrr_raymarch_bwd_workspace_bytes", "ndrr_last_error"} <= names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+    assert set(_ffi.SIGNATURES) >= declared_symbols()
+
+
+def test_abi_version_and_struct_layout(lib):
+    assert lib.ndrr_abi_version() == _ffi.ABI_VERSION
+    assert b"sm_103a" in lib.ndrr_build_info()
+    # 64-bit layout of ndrr_raymarch_args as declared in the header
+    assert ctypes.sizeof(_ffi.RaymarchArgs) == 248
+
+
+def _valid_args():
+    a = _ffi.RaymarchArgs()
+    a.vol = 0x1000
+    a.vol_dtype = _ffi.NDRR_F32
+    a.D, a.H, a.W = 8, 8, 8
+    a.n_classes = 1
+    a.M = a.src = a.tgt = a.step = 0x2000
+    a.B, a.N, a.width, a.n_samples = 2, 64, 8, 16
+    a.out = 0x3000
+    return a
+
+
+def test_workspace_query_needs_no_gpu(lib):
+    a = _valid_args()
+    nb = ctypes.c_uint64()
+    assert lib.ndrr_raymarch_bwd_workspace_bytes(ctypes.byref(a), ctypes.byref(nb)) == _ffi.NDRR_OK
+    # 8 x 8 image, default 16 x 8 tiles -> 1 tile per pose, 16 floats per tile
+    assert nb.value == 2 * 1 * 16 * 4
+
+
+@pytest.mark.parametrize(
+    "field,value,code,needle",
+    [
+        ("n_samples", 1, _ffi.NDRR_ERR_INVALID_ARGUMENT, "n_samples"),
+        ("vol_dtype", _ffi.NDRR_U8, _ffi.NDRR_ERR_DTYPE, "volume dtype"),
+        ("D", 0, _ffi.NDRR_ERR_INVALID_ARGUMENT, "dims"),
+        ("vol", None, _ffi.NDRR_ERR_INVALID_ARGUMENT, "vol is NULL"),
+        ("n_classes", 0, _ffi.NDRR_ERR_INVALID_ARGUMENT, "n_classes"),
+        ("n_classes", 3, _ffi.NDRR_ERR_INVALID_ARGUMENT, "label map"),
+        ("tile_w", 12, _ffi.NDRR_ERR_INVALID_ARGUMENT, "tile_w"),
+        ("sample_split", 3, _ffi.NDRR_ERR_INVALID_ARGUMENT, "sample_split"),
+        ("struct_size", 8, _ffi.NDRR_ERR_INVALID_ARGUMENT, "struct_size"),
+        ("out", None, _ffi.NDRR_ERR_INVALID_ARGUMENT, "out is NULL"),
+        ("tgt", None, _ffi.NDRR_ERR_INVALID_ARGUMENT, "non-NULL"),
+    ],
+)
+def test_forward_rejects_bad_arguments(lib, field, value, code, needle):
+    a = _valid_args()
+    setattr(a, field, value)
+    rc = lib.ndrr_raymarch_fwd(ctypes.byref(a), None)
+    assert rc == code
+    assert needle in lib.ndrr_last_error().decode()
+
+
+def test_int32_limits_rejected(lib):
+    a = _valid_args()
+    a.D, a.H, a.W = 2048, 1024, 1024  # 2^31 voxels
+    assert lib.ndrr_raymarch_fwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_LIMIT
+    a = _valid_args()
+    a.B, a.N = 65536, 65536
+    assert lib.ndrr_raymarch_fwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_LIMIT
+
+
+def test_empty_batch_is_a_no_op(lib):
+    a = _valid_args()
+    a.B = 0
+    a.M = a.src = a.tgt = a.step = None
+    assert lib.ndrr_raymarch_fwd(ctypes.byref(a), None) == _ffi.NDRR_OK
+
+
+def test_backward_rejects_missing_outputs_and_workspace(lib):
+    a = _valid_args()
+    a.go = 0x4000
+    a.go_dtype = _ffi.NDRR_F32
+    assert lib.ndrr_raymarch_bwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT  # gM NULL
+    a.gM = 0x5000
+    a.need_gvol = 1
+    assert lib.ndrr_raymarch_bwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT  # gvol NULL
+    a.need_gvol = 0
+    a.need_gcam = 1
+    assert lib.ndrr_raymarch_bwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT  # gsrc NULL
+    a.need_gcam = 0
+    assert lib.ndrr_raymarch_bwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_WORKSPACE
+    a.workspace = 0x6000
+    a.workspace_bytes = 8
+    assert lib.ndrr_raymarch_bwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_WORKSPACE
+    assert "workspace" in lib.ndrr_last_error().decode()
+
+
+def test_status_codes_map_to_reference_exceptions(lib):
+    a = _valid_args()
+    a.n_samples = 1
+    with pytest.raises(ValueError, match="n_samples"):
+        _ffi.check(lib.ndrr_raymarch_fwd(ctypes.byref(a), None), "fwd")
+    with pytest.raises(RuntimeError):
+        _ffi.check(_ffi.NDRR_ERR_CUDA, "fwd")

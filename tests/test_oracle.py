@@ -1,0 +1,155 @@
+"""The oracle, pinned against golden fixtures produced by the reference itself
+(tests/golden/make_golden.py runs nanodrr's `render(..., backend="torch")`).
+
+CPU only. The two restatements (grid_sample form and voxel-index numpy form)
+must reproduce the reference's outputs and gradients before any GPU result
+is compared against them.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import make_src, make_tgt, march_numpy, march_numpy_adjoint, render_oracle
+
+
+def _rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+def _geom(g, rt_key="rt_inv", ortho=False, dt=torch.float64):
+    H, W = int(g["height"]), int(g["width"])
+    k_inv = torch.from_numpy(g["k_inv"]).to(dt)
+    sdd = torch.from_numpy(g["sdd"]).to(dt)
+    rt = torch.from_numpy(g[rt_key]).to(dt)
+    tgt = make_tgt(k_inv, sdd, H, W, dt)
+    src = make_src(ortho, tgt, sdd)
+    return rt, src, tgt, sdd, k_inv, H, W
+
+
+def test_impulse_golden(impulse):
+    g = impulse
+    vol = torch.from_numpy(g["vol"]).double()
+    out = render_oracle(
+        vol, None, torch.from_numpy(g["world_to_voxel"]), torch.from_numpy(g["rt_inv"]),
+        torch.from_numpy(g["src"]), torch.from_numpy(g["tgt"]), int(g["n_samples"]),
+    )
+    assert float(out) == pytest.approx(1.0, rel=1e-3, abs=1e-3)
+    assert float(out) == pytest.approx(float(g["out"].squeeze()), rel=1e-6)
+
+
+@pytest.mark.parametrize("ortho", [False, True])
+@pytest.mark.parametrize("C", [1, 3])
+@pytest.mark.parametrize("dt,tag,tol", [(torch.float64, "f64", 1e-12), (torch.float32, "f32", 1e-6)])
+def test_grid_oracle_forward_golden(random32, ortho, C, dt, tag, tol):
+    g = random32
+    rt, src, tgt, *_ = _geom(g, ortho=ortho, dt=dt)
+    vol = torch.from_numpy(g["vol"]).to(dt)
+    lab = torch.from_numpy(g["lab"]).to(dt)
+    out = render_oracle(vol, lab, torch.from_numpy(g["world_to_voxel"]), rt, src, tgt, int(g["n_samples"]), C)
+    ref = g[f"fwd_{'ortho' if ortho else 'persp'}_c{C}_{tag}"].reshape(out.shape)
+    assert _rel(out.numpy(), ref) < tol
+
+
+@pytest.mark.parametrize("C", [1, 3])
+def test_grid_oracle_broadcast_golden(random32, C):
+    g = random32
+    rt, src, tgt, *_ = _geom(g, rt_key="rt_inv2")
+    out = render_oracle(
+        torch.from_numpy(g["vol"]).double(), torch.from_numpy(g["lab"]).double(),
+        torch.from_numpy(g["world_to_voxel"]), rt, src, tgt, int(g["n_samples"]), C,
+    )
+    assert _rel(out.numpy(), g[f"bcast_c{C}_f64"].reshape(out.shape)) < 1e-12
+
+
+@pytest.mark.parametrize("ortho", [False, True])
+def test_grid_oracle_pose_gradient_golden(random32, ortho):
+    g = random32
+    rt, src, tgt, *_ = _geom(g, ortho=ortho)
+    rt = rt.clone().requires_grad_(True)
+    vol = torch.from_numpy(g["vol"]).double()
+    # the camera-space rays do not depend on the pose
+    out = render_oracle(vol, None, torch.from_numpy(g["world_to_voxel"]), rt, src, tgt, int(g["n_samples"]))
+    (out.reshape(1, 1, 16, 16) * torch.from_numpy(g["w_pose"]).double()).sum().backward()
+    assert _rel(rt.grad.numpy()[0, :3], g[f"grt_{'ortho' if ortho else 'persp'}_f64"][0, :3]) < 1e-10
+
+
+def test_numpy_oracle_matches_golden(random32, phantom40):
+    """The voxel-index formulation equals the grid formulation (float64)."""
+    g = random32
+    rt, src, tgt, *_ = _geom(g)
+    w2v = torch.from_numpy(g["world_to_voxel"]).double()
+    M = (w2v @ rt)[:, :3].numpy()
+    step = ((tgt - src).norm(dim=-1) / (int(g["n_samples"]) - 1)).numpy()
+    for C in (1, 3):
+        out = march_numpy(g["vol"], g["lab"], M, src.numpy(), tgt.numpy(), step, int(g["n_samples"]), C)
+        assert _rel(out, g[f"fwd_persp_c{C}_f64"].reshape(out.shape)) < 1e-9
+    p = phantom40
+    rt, src, tgt, *_ = _geom(p, rt_key="rt_inv_rot")
+    M = (torch.from_numpy(p["world_to_voxel"]).double() @ rt)[:, :3].numpy()
+    step = ((tgt - src).norm(dim=-1) / (int(p["n_samples"]) - 1)).numpy()
+    for C in (1, 8):
+        out = march_numpy(p["vol"], p["lab"], M, src.numpy(), tgt.numpy(), step, int(p["n_samples"]), C)
+        ref = p[f"fwd_rot_c{C}_f64"].reshape(out.shape)
+        if C == 1:
+            assert _rel(out, ref) < 1e-9
+        else:
+            # nearest-label routing may flip exactly-half-way samples between
+            # formulations; channel sums must agree, flips must be rare
+            assert _rel(out.sum(1), ref.sum(1)) < 1e-9
+            bad = (np.abs(out - ref).max(1) / np.abs(ref).max()) > 1e-6
+            assert bad.mean() < 1e-2
+
+
+def test_numpy_adjoint_matches_golden_gradients(random32):
+    """Analytic adjoint (numpy) = reference autograd gradients (float64)."""
+    g = random32
+    n = int(g["n_samples"])
+    rt, src, tgt, *_ = _geom(g)
+    w2v = torch.from_numpy(g["world_to_voxel"]).double()
+    M = (w2v @ rt)[:, :3].numpy()
+    step = ((tgt - src).norm(dim=-1) / (n - 1)).numpy()
+    go = g["w_pose"].reshape(1, 1, -1).astype(np.float64)
+    gvol, gM, *_ = march_numpy_adjoint(go, g["vol"], None, M, src.numpy(), tgt.numpy(), step, n, 1)
+    # dL/drt_inv = world_to_voxel[:3]^T-chain: M = (w2v @ rt)[:3] -> grt = w2v[:3]^T gM
+    grt = w2v[:3].numpy().T @ gM[0]
+    assert _rel(grt[:3], g["grt_persp_f64"][0, :3]) < 1e-9
+    go3 = g["w_vol3"].reshape(1, 3, -1).astype(np.float64)
+    gvol3, *_ = march_numpy_adjoint(go3, g["vol"], g["lab"], M, src.numpy(), tgt.numpy(), step, n, 3)
+    assert _rel(gvol3, g["gvol_c3_f64"]) < 1e-9
+    go1 = g["w_vol1"].reshape(1, 1, -1).astype(np.float64)
+    gvol1, *_ = march_numpy_adjoint(go1, g["vol"], None, M, src.numpy(), tgt.numpy(), step, n, 1)
+    assert _rel(gvol1, g["gvol_c1_f64"]) < 1e-9
+
+
+def test_numpy_adjoint_camera_terms_central_differences():
+    """src/tgt/step gradients of the analytic adjoint vs central differences."""
+    rng = np.random.default_rng(0)
+    vol = rng.random((6, 7, 8))
+    M = np.array([[[1.0, 0.1, 0.0, 3.5], [0.0, 0.9, 0.2, 3.0], [0.1, 0.0, 1.1, 2.5]]])
+    src = np.array([[[-4.0, -3.5, -3.0]]])
+    tgt = rng.uniform(2.0, 6.0, size=(1, 5, 3))
+    step = rng.uniform(0.1, 0.2, size=(1, 5))
+    go = rng.standard_normal((1, 1, 5))
+    n = 40
+    f = lambda s, t, st, m: float((march_numpy(vol, None, m, s, t, st, n) * go).sum())  # noqa: E731
+    gvol, gM, gsrc, gtgt, gstep = march_numpy_adjoint(go, vol, None, M, src, tgt, step, n)
+    h = 1e-6
+    for arr_name, grad in (("tgt", gtgt), ("src", gsrc), ("step", gstep), ("M", gM)):
+        base = dict(s=src, t=tgt, st=step, m=M)
+        key = {"tgt": "t", "src": "s", "step": "st", "M": "m"}[arr_name]
+        num = np.zeros_like(base[key])
+        it = np.nditer(base[key], flags=["multi_index"])
+        for _ in it:
+            i = it.multi_index
+            plus, minus = base[key].copy(), base[key].copy()
+            plus[i] += h
+            minus[i] -= h
+            num[i] = (f(**{**base, key: plus}) - f(**{**base, key: minus})) / (2 * h)
+        assert _rel(grad, num) < 1e-5, arr_name
+    # volume: the forward is linear in the volume, so one difference is exact
+    e = np.zeros_like(vol)
+    e[3, 3, 4] = 1.0
+    fv = lambda v: float((march_numpy(v, None, M, src, tgt, step, n) * go).sum())  # noqa: E731
+    assert abs((fv(vol + e) - fv(vol - e)) / 2 - gvol[3, 3, 4]) < 1e-9

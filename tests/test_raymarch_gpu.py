@@ -1,0 +1,308 @@
+"""GPU parity of the CUDA ray march against the reference's outputs (golden
+fixtures generated by the reference) and the float64 oracle.
+
+Mirrors the reference's parity suite (tests/drr/test_fused.py:68-226) and
+known-answer test (tests/drr/test_renderer.py:52-91), with the north-star
+tolerances: float32 forward within 1e-5 relative max-abs of the float64
+reference, gradients within 1e-3, bf16/f16 volumes within 1e-2.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+from _gpu_helpers import assert_render_parity, np64, rays_for, rel_maxabs, subject_from_arrays
+
+import nanodrr_gb300 as nd
+from nanodrr_gb300 import _ffi
+from nanodrr_gb300.raymarch import raymarch_backward, raymarch_forward
+from oracle import march_numpy, march_numpy_adjoint
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+def test_single_ray_integral_equals_one(impulse):
+    g = impulse
+    sub = subject_from_arrays(g["vol"], None, g["voxel_to_world"], 1)
+    out = nd.render(
+        sub,
+        torch.as_tensor(g["k_inv"]).to(DEV),
+        torch.as_tensor(g["rt_inv"]).to(DEV),
+        torch.as_tensor(g["sdd"]).to(DEV),
+        1,
+        1,
+        n_samples=1001,
+        src=torch.as_tensor(g["src"]).to(DEV),
+        tgt=torch.as_tensor(g["tgt"]).to(DEV),
+    )
+    assert float(out) == pytest.approx(1.0, rel=1e-3, abs=1e-3)
+    assert float(out) == pytest.approx(float(g["out"].squeeze()), rel=1e-5)
+
+
+@pytest.mark.parametrize("orthographic", [False, True])
+@pytest.mark.parametrize("n_classes", [1, 3])
+def test_forward_matches_reference(random32, orthographic, n_classes):
+    g = random32
+    sub = subject_from_arrays(g["vol"], g["lab"], g["voxel_to_world"], n_classes)
+    k_inv, rt, sdd, H, W = rays_for(g)
+    out = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=int(g["n_samples"]), orthographic=orthographic)
+    assert out.shape == (1, n_classes, H, W)
+    key = f"fwd_{'ortho' if orthographic else 'persp'}_c{n_classes}"
+    assert_render_parity(g[key + "_f64"], out, n_classes, tol=1e-5)
+    assert_render_parity(g[key + "_f32"], out, n_classes, tol=1e-4)
+
+
+@pytest.mark.parametrize("orthographic", [False, True])
+def test_pose_gradients_match_reference(random32, orthographic):
+    g = random32
+    sub = subject_from_arrays(g["vol"], None, g["voxel_to_world"], 1)
+    k_inv, rt, sdd, H, W = rays_for(g)
+    rt = rt.clone().requires_grad_(True)
+    out = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=int(g["n_samples"]), orthographic=orthographic)
+    (out * torch.as_tensor(g["w_pose"]).to(DEV)).sum().backward()
+    ref = g[f"grt_{'ortho' if orthographic else 'persp'}_f64"][0, :3]
+    assert rel_maxabs(rt.grad[0, :3], ref) < 1e-3
+
+
+@pytest.mark.parametrize("n_classes", [1, 3])
+def test_volume_gradients_match_reference(random32, n_classes):
+    g = random32
+    sub = subject_from_arrays(g["vol"], g["lab"], g["voxel_to_world"], n_classes)
+    sub._image_hu = sub._image_hu.detach().requires_grad_(True)
+    k_inv, rt, sdd, H, W = rays_for(g)
+    out = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=int(g["n_samples"]))
+    w = g["w_vol1"] if n_classes == 1 else g["w_vol3"]
+    (out * torch.as_tensor(w).to(DEV)).sum().backward()
+    assert rel_maxabs(sub._image_hu.grad[0, 0], g[f"gvol_c{n_classes}_f64"]) < 1e-3
+
+
+def test_intrinsics_gradients_match_reference(random32):
+    g = random32
+    sub = subject_from_arrays(g["vol"], None, g["voxel_to_world"], 1)
+    k_inv, rt, sdd, H, W = rays_for(g)
+    k = k_inv.clone().requires_grad_(True)
+    s = sdd.clone().requires_grad_(True)
+    out = nd.render(sub, k, rt, s, H, W, n_samples=int(g["n_samples"]))
+    (out * torch.as_tensor(g["w_intr"]).to(DEV)).sum().backward()
+    assert rel_maxabs(k.grad, g["gk_f64"]) < 1e-3
+    assert rel_maxabs(s.grad, g["gsdd_f64"]) < 1e-3
+
+
+def test_pose_gradients_bitwise_deterministic(random32):
+    g = random32
+    sub = subject_from_arrays(g["vol"], None, g["voxel_to_world"], 1)
+    k_inv, rt_inv, sdd, H, W = rays_for(g)
+    w = torch.as_tensor(g["w_pose"]).to(DEV)
+    grads = []
+    for _ in range(3):
+        rt = rt_inv.clone().requires_grad_(True)
+        (nd.render(sub, k_inv, rt, sdd, H, W, n_samples=200) * w).sum().backward()
+        grads.append(rt.grad.clone())
+    torch.testing.assert_close(grads[0], grads[1], rtol=0, atol=0)
+    torch.testing.assert_close(grads[0], grads[2], rtol=0, atol=0)
+
+
+@pytest.mark.parametrize("n_classes", [1, 3])
+def test_pose_batch_broadcast(random32, n_classes):
+    g = random32
+    sub = subject_from_arrays(g["vol"], g["lab"], g["voxel_to_world"], n_classes)
+    k_inv, rt2, sdd, H, W = rays_for(g, rt_key="rt_inv2")
+    out = nd.render(sub, k_inv, rt2, sdd, H, W, n_samples=200)
+    assert out.shape == (2, n_classes, H, W)
+    assert_render_parity(g[f"bcast_c{n_classes}_f64"], out, n_classes, tol=1e-5)
+
+
+def test_out_of_range_labels_are_safe(random32):
+    g = random32
+    lab = (np.arange(g["lab"].size).reshape(g["lab"].shape) % 5).astype(np.float32)
+    sub = subject_from_arrays(g["vol"], lab, g["voxel_to_world"], 5)
+    sub.n_classes = 3  # fewer channels than the label map holds
+    k_inv, rt, sdd, H, W = rays_for(g)
+    rt = rt.clone().requires_grad_(True)
+    out = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=200)
+    out.sum().backward()
+    assert out.shape[1] == 3
+    assert torch.isfinite(out).all() and torch.isfinite(rt.grad).all()
+    # dropped labels contribute nothing: channel sum < unrouted integral
+    total = nd.render(subject_from_arrays(g["vol"], None, g["voxel_to_world"], 1), k_inv, rt.detach(), sdd, H, W,
+                      n_samples=200)
+    assert (out.sum(1) <= total[:, 0] * (1 + 1e-5) + 1e-6).all()
+
+
+@pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16])
+def test_half_volume_variants_within_1e_2(random32, dtype):
+    g = random32
+    for C in (1, 3):
+        sub = subject_from_arrays(g["vol"], g["lab"], g["voxel_to_world"], C, dtype=dtype)
+        k_inv, rt, sdd, H, W = rays_for(g)
+        out = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=200)
+        assert out.dtype == dtype
+        assert_render_parity(g[f"fwd_persp_c{C}_f64"], out.float(), C, tol=1e-2)
+
+
+@pytest.mark.parametrize("C", [1, 8])
+@pytest.mark.parametrize("pose", ["id", "rot"])
+def test_phantom_matches_reference(phantom40, C, pose):
+    g = phantom40
+    sub = subject_from_arrays(g["vol"], g["lab"], g["voxel_to_world"], C)
+    k_inv, rt, sdd, H, W = rays_for(g, rt_key="rt_inv" if pose == "id" else "rt_inv_rot")
+    out = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=int(g["n_samples"]))
+    assert_render_parity(g[f"fwd_{pose}_c{C}_f64"], out, C, tol=1e-5)
+
+
+def test_deterministic_mode_rejects_volume_gradients(random32):
+    g = random32
+    sub = subject_from_arrays(g["vol"], None, g["voxel_to_world"], 1)
+    sub._image_hu = sub._image_hu.detach().requires_grad_(True)
+    k_inv, rt, sdd, H, W = rays_for(g)
+    torch.use_deterministic_algorithms(True)
+    try:
+        out = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=50)
+        with pytest.raises(RuntimeError, match="nondeterministic"):
+            out.sum().backward()
+    finally:
+        torch.use_deterministic_algorithms(False)
+
+
+def test_compiles_with_gradients(random32):
+    """The custom ops trace opaquely under torch.compile (fake kernels)."""
+    g = random32
+    sub = subject_from_arrays(g["vol"], None, g["voxel_to_world"], 1)
+    k_inv, rt_inv, sdd, H, W = rays_for(g)
+    w = torch.as_tensor(g["w_pose"]).to(DEV)
+
+    def f(rt):
+        return nd.render(sub, k_inv, rt, sdd, H, W, n_samples=200)
+
+    rt = rt_inv.clone().requires_grad_(True)
+    (f(rt) * w).sum().backward()
+    torch._dynamo.reset()
+    rt_c = rt_inv.clone().requires_grad_(True)
+    (torch.compile(f, fullgraph=True, backend="aot_eager")(rt_c) * w).sum().backward()
+    assert rel_maxabs(rt_c.grad[0, :3], rt.grad[0, :3]) < 1e-6
+
+
+# ----------------------------------------------------------------- op level
+def _random_case(seed, B=3, Hd=20, Wd=24, vol_shape=(40, 36, 44), ortho=False, C=1):
+    rng = np.random.default_rng(seed)
+    vol = rng.random(vol_shape).astype(np.float32)
+    lab = rng.integers(0, C + 1, size=vol_shape).astype(np.uint8)
+    D, H, W = vol_shape
+    M = np.zeros((B, 3, 4), np.float32)
+    for b in range(B):
+        q, _ = np.linalg.qr(rng.standard_normal((3, 3)))
+        M[b, :, :3] = q * rng.uniform(0.8, 1.2)
+        M[b, :, 3] = np.array([W, H, D]) / 2 + rng.uniform(-3, 3, 3)
+    N = Hd * Wd
+    u, v = np.meshgrid(np.arange(Wd) - Wd / 2 + 0.5, np.arange(Hd) - Hd / 2 + 0.5)
+    tgt = np.stack([u.ravel() * 2.0, v.ravel() * 2.0, np.full(N, 60.0)], -1)[None].repeat(B, 0).astype(np.float32)
+    if ortho:
+        src = tgt.copy()
+        src[..., 2] = -60.0
+    else:
+        src = np.zeros((B, 1, 3), np.float32)
+        src[..., 2] = -60.0
+    step = (np.linalg.norm(tgt - src, axis=-1) / 199).astype(np.float32)
+    return vol, lab, M, src, tgt, step, Wd
+
+
+@pytest.mark.parametrize("ortho", [False, True])
+@pytest.mark.parametrize("C", [1, 4])
+def test_op_forward_and_adjoint_vs_numpy_oracle(ortho, C):
+    n = 200
+    vol, lab, M, src, tgt, step, width = _random_case(7, ortho=ortho, C=C)
+    t = lambda a: torch.from_numpy(a).to(DEV)  # noqa: E731
+    out, total = raymarch_forward(t(vol), t(lab), t(M), t(src), t(tgt), t(step), n, C, width, with_total=True)
+    ref = march_numpy(vol, lab, M, src, tgt, step, n, C)
+    assert_render_parity(ref, out, C, tol=1e-5)
+    ref1 = march_numpy(vol, lab, M, src, tgt, step, n, 1)
+    assert rel_maxabs(total, ref1[:, 0]) < 1e-5
+    rng = np.random.default_rng(3)
+    go = rng.standard_normal(out.shape).astype(np.float32)
+    gvol, gM, gsrc, gtgt, gstep = raymarch_backward(
+        t(go), t(vol), t(lab), t(M), t(src), t(tgt), t(step), n, C, width, True, True
+    )
+    rg = march_numpy_adjoint(go, vol, lab, M, src, tgt, step, n, C)
+    for name, mine, theirs in zip(("gvol", "gM", "gsrc", "gtgt", "gstep"), (gvol, gM, gsrc, gtgt, gstep), rg):
+        assert rel_maxabs(mine, theirs) < 1e-3, name
+
+
+@pytest.mark.parametrize("tile", [(8, 4, 1), (8, 8, 2), (16, 8, 4), (16, 16, 2), (32, 8, 1)])
+def test_launch_shapes_agree_through_the_c_abi(tile):
+    """Every tile shape / sample split gives the same image (C-ABI direct)."""
+    n = 150
+    vol, lab, M, src, tgt, step, width = _random_case(11, B=2, Hd=17, Wd=23, C=3)
+    t = lambda a: torch.from_numpy(a).to(DEV)  # noqa: E731
+    ref, _ = raymarch_forward(t(vol), t(lab), t(M), t(src), t(tgt), t(step), n, 3, width)
+    dv, dl, dM, ds, dt_, dst = t(vol), t(lab), t(M), t(src), t(tgt), t(step)
+    out = torch.empty_like(ref)
+    a = _ffi.RaymarchArgs()
+    a.vol, a.vol_dtype, (a.D, a.H, a.W) = dv.data_ptr(), _ffi.NDRR_F32, vol.shape
+    a.lab, a.lab_dtype, a.n_classes = dl.data_ptr(), _ffi.NDRR_U8, 3
+    a.M, a.src, a.tgt, a.step = dM.data_ptr(), ds.data_ptr(), dt_.data_ptr(), dst.data_ptr()
+    a.src_per_ray, a.B, a.N, a.width, a.n_samples = 0, 2, tgt.shape[1], width, n
+    a.out, a.out_dtype = out.data_ptr(), _ffi.NDRR_F32
+    a.tile_w, a.tile_h, a.sample_split = tile
+    lib = _ffi.load()
+    rc = lib.ndrr_raymarch_fwd(ctypes.byref(a), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0, lib.ndrr_last_error()
+    torch.cuda.synchronize()
+    assert rel_maxabs(out, ref) < 1e-6
+
+
+def test_linear_ray_list_and_per_ray_sources():
+    """width that does not divide N -> flat ray list; per-ray sources."""
+    n = 120
+    vol, lab, M, src, tgt, step, width = _random_case(5, B=2, ortho=True)
+    tgt, src, step = tgt[:, :451], src[:, :451], step[:, :451]
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(DEV)  # noqa: E731
+    out, _ = raymarch_forward(t(vol), t(lab), t(M), t(src), t(tgt), t(step), n, 1, 0)
+    ref = march_numpy(vol, lab, M, src, tgt, step, n, 1)
+    assert rel_maxabs(out, ref) < 1e-5
+
+
+def test_sample_window_restricts_the_march():
+    n = 100
+    vol, lab, M, src, tgt, step, width = _random_case(9, B=1)
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(DEV)  # noqa: E731
+    N = tgt.shape[1]
+    win = np.zeros((1, N, 2), np.float32)
+    win[..., 0] = 0.25
+    win[..., 1] = 0.75
+    out, _ = raymarch_forward(t(vol), t(lab), t(M), t(src), t(tgt), t(step), n, 1, width, t_window=t(win))
+    # only samples s with 0.25 <= s/(n-1) <= 0.75 count
+    s = np.arange(n) / (n - 1)
+    keep = (s >= 0.25) & (s <= 0.75)
+    full = np.zeros((1, 1, N))
+    for i in range(N):
+        ts = s[keep]
+        q = src[0, 0] + ts[:, None] * (tgt[0, i] - src[0, 0])
+        p = q @ M[0, :, :3].T + M[0, :, 3]
+        from oracle.numpy_oracle import _taps, _value
+
+        vals, fx, fy, fz = _taps(vol.astype(np.float64), p[:, 0], p[:, 1], p[:, 2])
+        full[0, 0, i] = _value(vals, fx, fy, fz).sum() * step[0, i]
+    assert rel_maxabs(out, full) < 1e-5
+
+
+def test_volume_adjoint_dot_product_identity():
+    """<go, A vol> == <A^T go, vol>: the volume adjoint is the exact transpose."""
+    n = 160
+    vol, lab, M, src, tgt, step, width = _random_case(13, B=2, C=1)
+    t = lambda a: torch.from_numpy(a).to(DEV)  # noqa: E731
+    out, _ = raymarch_forward(t(vol), t(lab), t(M), t(src), t(tgt), t(step), n, 1, width)
+    go = torch.randn_like(out)
+    gvol, *_ = raymarch_backward(go, t(vol), t(lab), t(M), t(src), t(tgt), t(step), n, 1, width, True, False)
+    lhs = (go.double() * out.double()).sum().item()
+    rhs = (gvol.double() * t(vol).double()).sum().item()
+    assert abs(lhs - rhs) / abs(lhs) < 1e-5
+
+
+def test_empty_batch_and_no_rays():
+    vol = torch.rand(4, 4, 4, device=DEV)
+    M = torch.zeros(0, 3, 4, device=DEV)
+    z3 = torch.zeros(0, 5, 3, device=DEV)
+    out, _ = raymarch_forward(vol, vol, M, torch.zeros(0, 1, 3, device=DEV), z3, torch.zeros(0, 5, device=DEV), 10, 1, 5)
+    assert out.shape == (0, 1, 5)
