@@ -55,6 +55,9 @@ def parse_args():
     p.add_argument("--samples", type=int, default=800)
     p.add_argument("--cpu-rays", type=int, default=2048, help="rays per CPU-baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--method", default="learned", choices=["plain", "occupancy", "learned"])
+    p.add_argument("--train-poses", type=int, default=16)
+    p.add_argument("--prop-epochs", type=int, default=40)
     return p.parse_args()
 
 
@@ -195,9 +198,10 @@ def count_samples(M, src, tgt, D, H, W, S):
 def run_ours(args, world, rank, local):
     import nanodrr_gb300 as nd
     from nanodrr_gb300 import _build
+    from nanodrr_gb300.empty_space import EmptySpace, train_proposal
     from nanodrr_gb300.raymarch import raymarch_backward, raymarch_forward
     from nanodrr_gb300.registration import NormalizedCrossCorrelation2d, Registration
-    from nanodrr_gb300.renderer import _make_src, _make_tgt
+    from nanodrr_gb300.renderer import _affine_product, _make_src, _make_tgt
 
     _build.build()
     dev = torch.device("cuda", local)
@@ -207,40 +211,77 @@ def run_ours(args, world, rank, local):
     del ph
     vol_param = sub._image_hu.detach().requires_grad_(True)
     sub._image_hu = vol_param
+    vol = vol_param.detach()[0, 0]
+    D, H, W = vol.shape
     k_inv, sdd, rt, held = k_inv.to(dev), sdd.to(dev), rt.to(dev), held.to(dev)
     B, Hd, S = args.batch, args.det, args.samples
     with torch.no_grad():
         target = nd.render(sub, k_inv, held, sdd, Hd, Hd, n_samples=S)
     ncc = NormalizedCrossCorrelation2d()
     reg = Registration(sub, rt, k_inv, sdd, Hd, Hd, batch=B).to(dev)
+    tgt = _make_tgt(k_inv, sdd, Hd, Hd, dev, torch.float32)
+    src = _make_src(False, tgt, sdd)
 
-    def step():
-        vol_param.grad = None
-        reg._rot.grad = None
-        reg._xyz.grad = None
-        img = reg(n_samples=S)
-        loss = -ncc(img, target).mean()
-        loss.backward()
-        return loss
+    # ---- learned proposal: labels from the plain renderer on training poses
+    # (a seed disjoint from the benchmark poses), fitted by the project's
+    # training kernels; then the occupancy grid that checks it.
+    from nanodrr_gb300 import phantom
 
-    for _ in range(max(args.warmup, 3)):
-        step()
+    t0 = time.perf_counter()
+    rt_train = phantom.random_poses(args.train_poses, seed=500 + rank).to(dev)
+    Mt = _affine_product(sub.world_to_voxel[:3], rt_train).contiguous()
+    tgt_t = tgt.expand(args.train_poses, -1, -1).contiguous()
+    src_t = src.expand(args.train_poses, -1, -1).contiguous()
+    step_t = ((tgt_t - src_t).norm(dim=-1) / (S - 1)).contiguous()
+    net, hist = train_proposal(vol, Mt, src_t, tgt_t, step_t, S, Hd, epochs=args.prop_epochs, batch=65536,
+                               lr=2e-3, alpha=20.0)
+    skips = {
+        "plain": None,
+        "occupancy": EmptySpace.occupancy(vol, cell=4),
+        "learned": EmptySpace.proposal(vol, net, cell=4, margin=2.0),
+    }
     torch.cuda.synchronize()
+    prep_s = time.perf_counter() - t0
 
-    # ---- device-timed steps (inputs resident in HBM)
+    def make_step(skip, vol_grad):
+        def step():
+            sub.empty_space = skip
+            vol_param.grad = None
+            reg._rot.grad = None
+            reg._xyz.grad = None
+            sub._image_hu = vol_param if vol_grad else vol_param.detach()
+            img = reg(n_samples=S)
+            loss = -ncc(img, target).mean()
+            loss.backward()
+            return loss
+
+        return step
+
+    def timed(fn, steps):
+        for _ in range(max(args.warmup, 3)):
+            fn()
+        barrier(world)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        barrier(world)
+        return max_over_ranks(e0.elapsed_time(e1) / 1e3, world, dev)
+
+    headline = args.method
     clocks = ClockSampler(torch.cuda.current_device())
-    barrier(world)
-    torch.cuda.synchronize()
     clocks.start()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    ev0.record()
-    for _ in range(args.steps):
-        step()
-    ev1.record()
-    torch.cuda.synchronize()
-    barrier(world)
+    table = {}
+    for name, skip in skips.items():
+        for vg in (True, False):
+            t = timed(make_step(skip, vg), args.steps)
+            table[f"{name}{'' if vg else '_pose_only'}"] = round(B * args.steps * world / t, 2)
+    # headline last, with the clocks still sampling
+    t_dev = timed(make_step(skips[headline], True), args.steps)
     clk = clocks.stop()
-    t_dev = max_over_ranks(ev0.elapsed_time(ev1) / 1e3, world, dev)
     frames = B * args.steps * world
     value = frames / t_dev
 
@@ -248,6 +289,7 @@ def run_ours(args, world, rank, local):
     # come from pinned host memory and the loss + pose gradients go back.
     host_params = torch.zeros(B, 6, pin_memory=True)
     host_out = torch.zeros(1 + B * 6, pin_memory=True)
+    step = make_step(skips[headline], True)
     barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -263,66 +305,76 @@ def run_ours(args, world, rank, local):
     t_e2e = max_over_ranks(time.perf_counter() - t0, world, dev)
     barrier(world)
     e2e = {
-        "value": frames / t_e2e,
+        "value": round(frames / t_e2e, 2),
         "unit": "frames/s",
         "h2d_bytes_per_step": host_params.numel() * 4,
         "d2h_bytes_per_step": host_out.numel() * 4,
     }
 
-    # ---- per-kernel timing for the roofline (same inputs, on the launch stream)
+    # ---- per-kernel timing for the roofline, on the launch stream
     with torch.no_grad():
         pose = reg.pose.detach()
-        M = (sub.world_to_voxel @ pose)[:, :3].contiguous()
-        tgt = _make_tgt(k_inv, sdd, Hd, Hd, dev, torch.float32).expand(B, -1, -1).contiguous()
-        src = _make_src(False, tgt, sdd.expand(B)).contiguous()
-        stepsz = ((tgt - src).norm(dim=-1) / (S - 1)).contiguous()
-        vol = sub.image[0, 0].detach()
-        D, H, W = vol.shape
+        M = _affine_product(sub.world_to_voxel[:3], pose).contiguous()
+        tgtb = tgt.expand(B, -1, -1).contiguous()
+        srcb = src.expand(B, -1, -1).contiguous()
+        stepsz = ((tgtb - srcb).norm(dim=-1) / (S - 1)).contiguous()
         go = torch.randn(B, 1, Hd * Hd, device=dev)
-        n_samp = count_samples(M, src, tgt, D, H, W, S)
+        n_samp = count_samples(M, srcb, tgtb, D, H, W, S)
+        stats = torch.zeros(4, dtype=torch.int64, device=dev)
+        raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, skip=skips["learned"], stats=stats)
+        occ_stats = torch.zeros(4, dtype=torch.int64, device=dev)
+        raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, skip=skips["occupancy"], stats=occ_stats)
         gvol = torch.zeros_like(vol)
         reps = max(3, args.steps)
-        fwd_ms, bwd_ms = [], []
+        times = {"fwd": [], "fwd_learned": [], "bwd": []}
         for i in range(reps + 1):
-            e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
             e[0].record()
-            raymarch_forward(vol, vol, M, src, tgt, stepsz, S, 1, Hd)
+            raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd)
             e[1].record()
+            raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, skip=skips["learned"])
             e[2].record()
-            raymarch_backward(go, vol, vol, M, src, tgt, stepsz, S, 1, Hd, True, True, gvol=gvol)
             e[3].record()
+            raymarch_backward(go, vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, True, True, gvol=gvol)
+            e[4].record()
             torch.cuda.synchronize()
             if i > 0:
-                fwd_ms.append(e[0].elapsed_time(e[1]))
-                bwd_ms.append(e[2].elapsed_time(e[3]))
+                times["fwd"].append(e[0].elapsed_time(e[1]))
+                times["fwd_learned"].append(e[1].elapsed_time(e[2]))
+                times["bwd"].append(e[3].elapsed_time(e[4]))
     e_bytes = vol.element_size()
     fwd_bytes = n_samp * 8 * e_bytes
     bwd_bytes = n_samp * (8 * e_bytes + 4 + 8 * 4 * 2)
-    fwd_s, bwd_s = statistics.median(fwd_ms) / 1e3, statistics.median(bwd_ms) / 1e3
+    fwd_s = statistics.median(times["fwd"]) / 1e3
+    bwd_s = statistics.median(times["bwd"]) / 1e3
+    fwdl_s = statistics.median(times["fwd_learned"]) / 1e3
     peaks = _peaks()
-    dominant = ("bwd", bwd_bytes, bwd_s) if bwd_s >= fwd_s else ("fwd", fwd_bytes, fwd_s)
-    achieved = dominant[1] / dominant[2] / 1e9
+    achieved = bwd_bytes / bwd_s / 1e9
+    st = stats.tolist()
+    ost = occ_stats.tolist()
     roofline = {
         "bound": "hbm",
-        "kernel": f"raymarch_{dominant[0]}_kernel",
+        "kernel": "raymarch_bwd_brick_kernel (adjoint with volume gradient)",
         "achieved": round(achieved, 1),
         "peak": peaks["hbm_gbs"],
         "peak_source": peaks["source"],
         "unit": "GB/s",
         "frac": round(achieved / peaks["hbm_gbs"], 4),
         "traffic": None,
-        "algorithmic_bytes_per_launch": dominant[1],
+        "algorithmic_bytes_per_launch": bwd_bytes,
         "samples_per_launch": n_samp,
         "fwd_ms": round(fwd_s * 1e3, 3),
+        "fwd_learned_ms": round(fwdl_s * 1e3, 3),
         "bwd_ms": round(bwd_s * 1e3, 3),
         "fwd_gsamples_per_s": round(n_samp / fwd_s / 1e9, 2),
         "bwd_gsamples_per_s": round(n_samp / bwd_s / 1e9, 2),
+        "fwd_frac_of_hbm": round(fwd_bytes / fwd_s / 1e9 / peaks["hbm_gbs"], 4),
     }
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, sub, k_inv, sdd, rt)
     out = {
-        "metric": "fwd+bwd DRR frames/s at 512^3/256^2 (plain CUDA kernel)",
+        "metric": "fwd+bwd DRR frames/s at 512^3/256^2, learned-skip vs plain kernel",
         "value": round(value, 2),
         "unit": "frames/s",
         "n_gpus": world,
@@ -340,9 +392,22 @@ def run_ours(args, world, rank, local):
                 f"{Hd}x{Hd} detector ({args.pixel} mm), {S} samples/ray, fwd + NCC + bwd to se(3) "
                 "6-vector and volume"
             ),
-            "method": "plain kernel (box-culled march)",
+            "method": f"{headline} ({'learned proposal + occupancy check' if headline == 'learned' else headline})",
             "l2": "inputs larger than L2 (volume and its gradient 512 MiB each)",
             "parallelism": f"replicas x{world}",
+        },
+        "methods_frames_per_s": table,
+        "learned_vs_plain": round(table["learned"] / table["plain"], 3),
+        "learned_vs_plain_pose_only": round(table["learned_pose_only"] / table["plain_pose_only"], 3),
+        "proposal": {
+            "train_poses": args.train_poses,
+            "train_rays": args.train_poses * Hd * Hd,
+            "epochs": args.prop_epochs,
+            "loss_first_last": [round(hist[0], 5), round(hist[-1], 5)],
+            "prep_s": round(prep_s, 2),
+            "fallback_fraction": round(st[1] / max(1, st[0]), 4),
+            "marched_over_box_samples": round(st[2] / max(1, st[3]), 4),
+            "occupancy_marched_over_box_samples": round(ost[2] / max(1, ost[3]), 4),
         },
         "samples_per_s": round(n_samp * args.steps * world / t_dev, 1),
         "roofline": roofline,

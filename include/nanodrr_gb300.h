@@ -126,12 +126,53 @@ typedef struct ndrr_raymarch_args {
     void* workspace;
     uint64_t workspace_bytes;
 
+    /* Empty-space skipping (optional; see ndrr_occupancy_build).
+     * skip_mode NDRR_SKIP_OCCUPANCY: each ray marches only between the first
+     * and last occupied grid cell it crosses. NDRR_SKIP_PROPOSAL: the learned
+     * proposal network (proposal_params, packed by ndrr_proposal_pack)
+     * predicts the non-empty interval inside the render kernel; the
+     * occupancy grid then checks that nothing occupied lies outside it, and
+     * rays that fail the check march their full box-culled window. Skipped
+     * samples have eight zero corners, so the image and the pose and camera
+     * gradients are unchanged; the volume gradient, which is non-zero on
+     * empty voxels too, always uses the full window (the adjoint ignores the
+     * skip when need_gvol is set). */
+    int32_t skip_mode;
+    int32_t occ_cell;
+    int32_t occ_gx, occ_gy, occ_gz;
+    const uint8_t* occ_grid;
+    const void* proposal_params;
+    float proposal_margin;          /* widening of a proposed interval, samples */
+    unsigned long long* skip_stats; /* optional [4] counters, accumulated: rays
+                                       with a window, rays sent to the full
+                                       march, samples marched, samples in the
+                                       box-culled windows */
+    float* out_extent;              /* optional [B, N, 2] forward output: t of
+                                       the first and last sample with a
+                                       non-zero corner, (1, 0) when none */
+
     /* Launch tuning; 0 selects the library default for each. */
     int32_t tile_w;         /* detector tile width in rays (8 or 16)            */
     int32_t tile_h;         /* detector tile height in rays (8 or 16)           */
     int32_t sample_split;   /* 1, 2 or 4 sample chunks per ray within a CTA     */
-    int32_t reserved[5];
+    int32_t gvol_mode;      /* adjoint volume-gradient scatter: 0 auto,
+                               1 direct global atomics per tap, 2 per-slab
+                               shared-memory brick flushed with coalesced
+                               atomics (NDRR_GVOL_*)                            */
+    int32_t reserved[4];
 } ndrr_raymarch_args;
+
+enum ndrr_skip_mode {
+    NDRR_SKIP_NONE = 0,
+    NDRR_SKIP_OCCUPANCY = 1,
+    NDRR_SKIP_PROPOSAL = 2,
+};
+
+enum ndrr_gvol_mode {
+    NDRR_GVOL_AUTO = 0,
+    NDRR_GVOL_DIRECT = 1,
+    NDRR_GVOL_BRICK = 2,
+};
 
 /* Library identity. */
 NDRR_API int32_t ndrr_abi_version(void);
@@ -157,6 +198,72 @@ NDRR_API int32_t ndrr_raymarch_bwd_workspace_bytes(const ndrr_raymarch_args* arg
  * pose, as the reference's _backward does at _fused.py:552-553) and
  * accumulates the volume gradient with atomics (not bitwise deterministic). */
 NDRR_API int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* args, void* stream);
+
+/* ---- empty-space structures ---------------------------------------------- */
+typedef struct ndrr_occupancy_args {
+    uint32_t struct_size;   /* sizeof(ndrr_occupancy_args) */
+    uint32_t abi_version;
+    const void* vol;        /* [D, H, W] f32 / f16 / bf16 */
+    int32_t vol_dtype;
+    int32_t D, H, W;
+    int32_t cell;           /* cell edge in voxels, 2..64 */
+    int32_t max_dist;       /* Chebyshev distance cap in cells, 1..255 */
+    uint8_t* grid;          /* [gz, gy, gx] output (ndrr_occupancy_dims) */
+    uint8_t* scratch;       /* [gz, gy, gx] scratch */
+} ndrr_occupancy_args;
+
+/* Grid extent for a volume: ceil(dim / cell) + 2 cells per axis (one border
+ * cell on each side). */
+NDRR_API int32_t ndrr_occupancy_dims(int32_t D, int32_t H, int32_t W, int32_t cell, int32_t* gz, int32_t* gy,
+                                     int32_t* gx);
+
+/* Build the occupancy / distance grid of a volume. Grid cell g spans voxels
+ * [(g - 1) cell, g cell) per axis and is occupied when any voxel within two
+ * voxels of it is non-zero; the grid stores the Chebyshev distance in cells
+ * to the nearest occupied cell (0 = occupied, capped at max_dist). No
+ * counterpart in the reference, which marches every box-culled sample. */
+NDRR_API int32_t ndrr_occupancy_build(const ndrr_occupancy_args* args, void* stream);
+
+/* ---- learned proposal network ---------------------------------------------
+ * 3-layer MLP 64 -> 64 -> 64 -> 2 on Fourier-encoded ray entry/exit points,
+ * predicting the fractions of the in-box segment where a ray's non-empty
+ * interval starts and ends. fp32 master parameters (NDRR_PROPOSAL_PARAMS
+ * floats: W1 [64][64], b1, W2 [64][64], b2, W3 [2][64], b3) are trained by the
+ * kernels below and packed to bf16 (NDRR_PROPOSAL_PACKED_BYTES) for the
+ * tensor-core inference inside the render kernels. No counterpart in the
+ * reference. */
+#define NDRR_PROPOSAL_PARAMS 8450
+#define NDRR_PROPOSAL_PACKED_BYTES 17952
+#define NDRR_PROPOSAL_FEATURES 64
+
+NDRR_API const char* ndrr_proposal_last_error(void);
+
+/* Features [B*N, 64] f32, targets [B*N, 2] f32 and valid [B*N] u8 for the rays
+ * described by `rays` (M, src, tgt, volume dims), from the per-ray non-empty
+ * interval `extent` [B, N, 2] that ndrr_raymarch_fwd writes to out_extent,
+ * widened by `widen_voxels` of Chebyshev distance on each side (use the
+ * occupancy cell size + 3 so that the check can confirm a correct proposal). */
+NDRR_API int32_t ndrr_proposal_dataset(const ndrr_raymarch_args* rays, const float* extent, float widen_voxels,
+                                       float* features, float* targets, uint8_t* valid, void* stream);
+
+/* Forward, asymmetric loss (clipping the target interval costs `alpha` times
+ * more than widening it) and backward over n rays; ACCUMULATES the gradient
+ * of inv_count * sum(loss) into grads [NDRR_PROPOSAL_PARAMS] and the loss
+ * into *loss. */
+NDRR_API int32_t ndrr_proposal_train_step(const float* params, const float* features, const float* targets,
+                                          const uint8_t* valid, int64_t n, float alpha, float inv_count,
+                                          float* grads, float* loss, void* stream);
+
+/* fp32 network outputs [n, 2]. */
+NDRR_API int32_t ndrr_proposal_forward(const float* params, const float* features, int64_t n, float* out,
+                                       void* stream);
+
+/* One Adam update of the master parameters (step >= 1 for bias correction). */
+NDRR_API int32_t ndrr_proposal_adam(float* params, const float* grads, float* m1, float* m2, int32_t step, float lr,
+                                    float beta1, float beta2, float eps, void* stream);
+
+/* Pack the fp32 master parameters into the bf16 inference layout. */
+NDRR_API int32_t ndrr_proposal_pack(const float* params, void* packed, void* stream);
 
 #ifdef __cplusplus
 }

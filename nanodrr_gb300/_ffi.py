@@ -27,6 +27,9 @@ NDRR_F32, NDRR_F16, NDRR_BF16, NDRR_U8, NDRR_I8, NDRR_I16, NDRR_I32, NDRR_I64 = 
 
 ABI_VERSION = 1
 
+# ndrr_gvol_mode
+NDRR_GVOL_AUTO, NDRR_GVOL_DIRECT, NDRR_GVOL_BRICK = 0, 1, 2
+
 _c_float_p = ctypes.POINTER(ctypes.c_float)
 
 
@@ -68,10 +71,21 @@ class RaymarchArgs(ctypes.Structure):
         ("gstep", ctypes.c_void_p),
         ("workspace", ctypes.c_void_p),
         ("workspace_bytes", ctypes.c_uint64),
+        ("skip_mode", ctypes.c_int32),
+        ("occ_cell", ctypes.c_int32),
+        ("occ_gx", ctypes.c_int32),
+        ("occ_gy", ctypes.c_int32),
+        ("occ_gz", ctypes.c_int32),
+        ("occ_grid", ctypes.c_void_p),
+        ("proposal_params", ctypes.c_void_p),
+        ("proposal_margin", ctypes.c_float),
+        ("skip_stats", ctypes.c_void_p),
+        ("out_extent", ctypes.c_void_p),
         ("tile_w", ctypes.c_int32),
         ("tile_h", ctypes.c_int32),
         ("sample_split", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 5),
+        ("gvol_mode", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 4),
     ]
 
     def __init__(self, **kw):
@@ -79,6 +93,34 @@ class RaymarchArgs(ctypes.Structure):
         self.struct_size = ctypes.sizeof(RaymarchArgs)
         self.abi_version = ABI_VERSION
 
+
+class OccupancyArgs(ctypes.Structure):
+    """Mirror of `ndrr_occupancy_args`."""
+
+    _fields_ = [
+        ("struct_size", ctypes.c_uint32),
+        ("abi_version", ctypes.c_uint32),
+        ("vol", ctypes.c_void_p),
+        ("vol_dtype", ctypes.c_int32),
+        ("D", ctypes.c_int32),
+        ("H", ctypes.c_int32),
+        ("W", ctypes.c_int32),
+        ("cell", ctypes.c_int32),
+        ("max_dist", ctypes.c_int32),
+        ("grid", ctypes.c_void_p),
+        ("scratch", ctypes.c_void_p),
+    ]
+
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        self.struct_size = ctypes.sizeof(OccupancyArgs)
+        self.abi_version = ABI_VERSION
+
+
+# ndrr_skip_mode
+NDRR_SKIP_NONE, NDRR_SKIP_OCCUPANCY, NDRR_SKIP_PROPOSAL = 0, 1, 2
+
+_i32p = ctypes.POINTER(ctypes.c_int32)
 
 # Every symbol the header declares, with its ctypes signature.
 SIGNATURES: dict[str, tuple] = {
@@ -91,6 +133,23 @@ SIGNATURES: dict[str, tuple] = {
         [ctypes.POINTER(RaymarchArgs), ctypes.POINTER(ctypes.c_uint64)],
     ),
     "ndrr_raymarch_bwd": (ctypes.c_int32, [ctypes.POINTER(RaymarchArgs), ctypes.c_void_p]),
+    "ndrr_occupancy_dims": (ctypes.c_int32, [ctypes.c_int32] * 4 + [_i32p] * 3),
+    "ndrr_occupancy_build": (ctypes.c_int32, [ctypes.POINTER(OccupancyArgs), ctypes.c_void_p]),
+    "ndrr_proposal_last_error": (ctypes.c_char_p, []),
+    "ndrr_proposal_dataset": (
+        ctypes.c_int32,
+        [ctypes.POINTER(RaymarchArgs), ctypes.c_void_p, ctypes.c_float] + [ctypes.c_void_p] * 4,
+    ),
+    "ndrr_proposal_train_step": (
+        ctypes.c_int32,
+        [ctypes.c_void_p] * 4 + [ctypes.c_int64, ctypes.c_float, ctypes.c_float] + [ctypes.c_void_p] * 3,
+    ),
+    "ndrr_proposal_forward": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64] + [ctypes.c_void_p] * 2),
+    "ndrr_proposal_adam": (
+        ctypes.c_int32,
+        [ctypes.c_void_p] * 4 + [ctypes.c_int32] + [ctypes.c_float] * 4 + [ctypes.c_void_p],
+    ),
+    "ndrr_proposal_pack": (ctypes.c_int32, [ctypes.c_void_p] * 3),
 }
 
 _lock = threading.Lock()

@@ -79,6 +79,24 @@ int32_t validate_common(const ndrr_raymarch_args* a) {
         return fail(NDRR_ERR_INVALID_ARGUMENT, "tile_h must be a multiple of 4 in [4, 64] (got %d)", a->tile_h);
     if (a->sample_split != 0 && a->sample_split != 1 && a->sample_split != 2 && a->sample_split != 4)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "sample_split must be 1, 2 or 4 (got %d)", a->sample_split);
+    if (a->skip_mode < NDRR_SKIP_NONE || a->skip_mode > NDRR_SKIP_PROPOSAL)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "skip_mode must be 0, 1 or 2 (got %d)", a->skip_mode);
+    if (a->skip_mode != NDRR_SKIP_NONE) {
+        if (a->occ_grid == nullptr || a->occ_cell < 2 || a->occ_cell > 64)
+            return fail(NDRR_ERR_INVALID_ARGUMENT, "skipping needs an occupancy grid with a cell of 2..64 voxels");
+        const int gx = (a->W + a->occ_cell - 1) / a->occ_cell + 2, gy = (a->H + a->occ_cell - 1) / a->occ_cell + 2,
+                  gz = (a->D + a->occ_cell - 1) / a->occ_cell + 2;
+        if (a->occ_gx != gx || a->occ_gy != gy || a->occ_gz != gz)
+            return fail(NDRR_ERR_INVALID_ARGUMENT, "occupancy grid %dx%dx%d does not match the volume (%dx%dx%d)",
+                        a->occ_gz, a->occ_gy, a->occ_gx, gz, gy, gx);
+        if (a->skip_mode == NDRR_SKIP_PROPOSAL && a->proposal_params == nullptr)
+            return fail(NDRR_ERR_INVALID_ARGUMENT, "proposal skipping needs packed proposal parameters");
+        if (!(a->proposal_margin >= 0.f)) return fail(NDRR_ERR_INVALID_ARGUMENT, "proposal_margin must be >= 0");
+    }
+    if (a->gvol_mode < NDRR_GVOL_AUTO || a->gvol_mode > NDRR_GVOL_BRICK)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode must be 0, 1 or 2 (got %d)", a->gvol_mode);
+    if (a->reserved[0] < 0 || a->reserved[0] > 56 * 1024)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "brick capacity %d out of range [0, 57344] voxels", a->reserved[0]);
     return NDRR_OK;
 }
 
@@ -111,7 +129,11 @@ int32_t ndrr_raymarch_fwd(const ndrr_raymarch_args* a, void* stream) {
     if (a->B == 0 || a->N == 0) return ok();
     if (a->out == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "out is NULL");
     if (!is_float_dtype(a->out_dtype)) return fail(NDRR_ERR_DTYPE, "out dtype %d unsupported", a->out_dtype);
+    if (a->skip_mode != NDRR_SKIP_NONE && a->out_dtype != a->vol_dtype)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "empty-space skipping writes the output in the volume's dtype");
     const ndrr::LaunchShape ls = ndrr::choose_shape(*a, sm_count_current());
+    if (a->skip_mode == NDRR_SKIP_PROPOSAL && ls.tw * ls.th * ls.K > 256)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "proposal skipping supports at most 256 threads per tile");
     rc = validate_shape(ls, ndrr::fwd_smem_bytes(*a, ls));
     if (rc != NDRR_OK) return rc;
     const cudaError_t e = ndrr::launch_fwd(*a, ls, reinterpret_cast<cudaStream_t>(stream));
@@ -149,10 +171,38 @@ int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* a, void* stream) {
         return fail(NDRR_ERR_WORKSPACE, "adjoint needs %llu workspace bytes, got %llu", (unsigned long long)need,
                     (unsigned long long)(a->workspace ? a->workspace_bytes : 0));
     const ndrr::LaunchShape ls = ndrr::choose_shape(*a, sm_count_current());
-    rc = validate_shape(ls, ndrr::bwd_smem_bytes(*a, ls));
+    rc = validate_shape(ls, (a->need_gvol && ls.brick) ? ndrr::brick_smem_bytes(*a, ls) : ndrr::bwd_smem_bytes(*a, ls));
     if (rc != NDRR_OK) return rc;
     const cudaError_t e = ndrr::launch_bwd(*a, ls, reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "adjoint launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
+int32_t ndrr_occupancy_dims(int32_t D, int32_t H, int32_t W, int32_t cell, int32_t* gz, int32_t* gy, int32_t* gx) {
+    if (gz == nullptr || gy == nullptr || gx == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "NULL output");
+    if (D < 1 || H < 1 || W < 1 || cell < 2 || cell > 64)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "dims must be positive and cell in 2..64");
+    *gz = (D + cell - 1) / cell + 2;
+    *gy = (H + cell - 1) / cell + 2;
+    *gx = (W + cell - 1) / cell + 2;
+    return ok();
+}
+
+int32_t ndrr_occupancy_build(const ndrr_occupancy_args* a, void* stream) {
+    if (a == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "args is NULL");
+    if (a->struct_size != sizeof(ndrr_occupancy_args) || a->abi_version != NDRR_ABI_VERSION)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "ndrr_occupancy_args size/version mismatch");
+    if (a->vol == nullptr || a->grid == nullptr || a->scratch == nullptr)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "vol, grid and scratch must be non-NULL");
+    if (!is_float_dtype(a->vol_dtype)) return fail(NDRR_ERR_DTYPE, "volume dtype %d unsupported", a->vol_dtype);
+    if (a->D < 1 || a->H < 1 || a->W < 1 || (long long)a->D * a->H * a->W >= kInt32Max)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "bad volume dims");
+    if (a->cell < 2 || a->cell > 64) return fail(NDRR_ERR_INVALID_ARGUMENT, "cell must be 2..64 (got %d)", a->cell);
+    if (a->max_dist < 1 || a->max_dist > 255)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "max_dist must be 1..255 (got %d)", a->max_dist);
+    const cudaError_t e = ndrr::launch_occupancy(a->vol, a->vol_dtype, a->D, a->H, a->W, a->cell, a->max_dist,
+                                                 a->grid, a->scratch, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "occupancy build failed: %s", cudaGetErrorString(e));
     return ok();
 }
 

@@ -12,14 +12,20 @@ struct LaunchShape {
     int tw = 16;  // tile width in rays (multiple of 8)
     int th = 8;   // tile height in rays (multiple of 4)
     int K = 1;    // sample chunks per ray within a CTA
+    bool brick = false;  // adjoint: per-slab shared-memory volume-gradient brick
+    int cap = 0;         // brick capacity in voxels
+    int L0 = 16;         // initial slab length in samples
 };
 
 LaunchShape choose_shape(const ndrr_raymarch_args& a, int sm_count);
 uint64_t bwd_workspace_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
 size_t fwd_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
 size_t bwd_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
+size_t brick_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
 
 cudaError_t launch_fwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
 cudaError_t launch_bwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
+cudaError_t launch_occupancy(const void* vol, int vol_dtype, int D, int H, int W, int cell, int max_dist,
+                             uint8_t* dist, uint8_t* scratch, cudaStream_t st);
 
 }  // namespace ndrr

@@ -1,0 +1,724 @@
+// Shared device code of the ray-march kernels: parameters, per-ray set-up,
+// empty-space skipping, the forward body and the adjoint bodies. The kernels
+// are templates instantiated by the launchers in ndrr_fwd.cu, ndrr_bwd.cu and
+// ndrr_brick.cu (separate translation units, compiled in parallel).
+//
+// Work decomposition: one CTA per (pose, detector tile). A tile is
+// tile_w x tile_h rays, each warp an 8 x 4 sub-patch so that its gathers hit a
+// compact footprint. Optionally each ray's sample window is split into
+// `sample_split` contiguous chunks marched by different threads of the same
+// CTA; the chunk partials are summed in shared memory in a fixed order, so the
+// result is deterministic and no global partial buffer or second pass is
+// needed for the forward (the reference writes split partials to global
+// memory and sums them in torch, nanodrr src/nanodrr/drr/_fused.py:436-459).
+//
+// Forward per sample (reference _fused.py:190-228, 300): trilinear tap with
+// zero padding, optional nearest-label routing, fp32 accumulation; the sum is
+// scaled by the per-ray step at the end (_fused.py:327-331).
+//
+// Adjoint per sample (reference _fused.py:230-298): recompute the tap, form
+// g = go[b, class, n] * step, the analytic trilinear position gradient, the
+// pose partial dL/dM_ij += g * dv_i * [q, 1]_j, optional camera-space
+// gradients, and the volume gradient scattered to the 8 corners by atomics.
+// Pose partials are reduced per CTA with a fixed shuffle tree and per pose by
+// a second small kernel in a fixed order, so gM is bitwise reproducible.
+#pragma once
+
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+
+#include "ndrr_device.cuh"
+#include "ndrr_launch.h"
+#include "ndrr_proposal.cuh"
+#include "ndrr_skip.cuh"
+
+namespace ndrr {
+
+struct MarchParams {
+    const void* vol;
+    int D, H, W;
+    const void* lab;
+    int lab_dtype;
+    int C;
+    const float* M;
+    const float* src;
+    const float* tgt;
+    const float* step;
+    int src_per_ray;
+    int B, N, S;
+    float inv_s;
+    const float* t_window;
+    // forward
+    void* out;
+    void* out_total;
+    // adjoint
+    const void* go;
+    int go_dtype;
+    float* gvol;
+    float* gsrc;
+    float* gtgt;
+    float* gstep;
+    float* partials;  // [B * tiles, kPartialStride]
+    // empty-space skipping
+    int skip_mode;
+    OccGrid occ;
+    const unsigned char* proposal;  // packed network parameters
+    float margin;                   // widening of a proposed interval (samples)
+    unsigned long long* stats;      // [4] counters or NULL
+    float* out_extent;              // [B, N, 2] or NULL
+    size_t prop_off;                // byte offset of the proposal smem region
+    // launch shape
+    TileMap tm;
+    int tw, th, K;
+};
+
+constexpr int kSkipSteps = 256;  // distance-field steps per query before giving up
+
+constexpr int kPartialStride = 16;  // 12 pose terms + 3 shared-source terms + pad
+
+// Per-thread ray set-up: voxel-space line, window, this thread's chunk.
+struct ThreadRay {
+    Ray ray;
+    int n;         // ray index or -1
+    size_t bn;     // b * N + n
+    float stepv;   // camera-space sample spacing
+    float sx, sy, sz, ex, ey, ez;  // camera-space source and src -> tgt
+    int s0, s1;    // this thread's sample chunk
+};
+
+// Box-culled ray set-up (every thread of a ray computes the same window).
+__device__ __forceinline__ void init_thread_ray(const MarchParams& p, const float (&m)[12], int b, int n,
+                                                ThreadRay& tr) {
+    tr.n = n;
+    tr.ray.lo = tr.ray.hi = 0;
+    tr.stepv = 0.f;
+    tr.sx = tr.sy = tr.sz = tr.ex = tr.ey = tr.ez = 0.f;
+    tr.ray.p0x = tr.ray.p0y = tr.ray.p0z = tr.ray.dx = tr.ray.dy = tr.ray.dz = 0.f;
+    tr.bn = 0;
+    if (n >= 0) {
+        const size_t bn = (size_t)b * p.N + n;
+        tr.bn = bn;
+        const float* sp = p.src_per_ray ? p.src + bn * 3 : p.src + (size_t)b * 3;
+        const float sx = __ldg(sp + 0), sy = __ldg(sp + 1), sz = __ldg(sp + 2);
+        const float tx = __ldg(p.tgt + bn * 3 + 0), ty = __ldg(p.tgt + bn * 3 + 1), tz = __ldg(p.tgt + bn * 3 + 2);
+        const float ex = tx - sx, ey = ty - sy, ez = tz - sz;
+        tr.sx = sx; tr.sy = sy; tr.sz = sz;
+        tr.ex = ex; tr.ey = ey; tr.ez = ez;
+        tr.ray.p0x = m[0] * sx + m[1] * sy + m[2] * sz + m[3];
+        tr.ray.p0y = m[4] * sx + m[5] * sy + m[6] * sz + m[7];
+        tr.ray.p0z = m[8] * sx + m[9] * sy + m[10] * sz + m[11];
+        tr.ray.dx = m[0] * ex + m[1] * ey + m[2] * ez;
+        tr.ray.dy = m[4] * ex + m[5] * ey + m[6] * ez;
+        tr.ray.dz = m[8] * ex + m[9] * ey + m[10] * ez;
+        ray_window(tr.ray, p.D, p.H, p.W, p.S);
+        if (p.t_window) apply_t_window(tr.ray, __ldg(p.t_window + bn * 2), __ldg(p.t_window + bn * 2 + 1), p.S);
+        tr.stepv = __ldg(p.step + bn);
+    }
+    tr.s0 = tr.ray.lo;
+    tr.s1 = tr.ray.hi;
+}
+
+// This thread's share [s0, s1) of the ray's window when K threads split it.
+__device__ __forceinline__ void chunk_thread_ray(ThreadRay& tr, int k, int K) {
+    const int len = max(tr.ray.hi - tr.ray.lo, 0);
+    const int chunk = (len + K - 1) / K;
+    tr.s0 = tr.ray.lo + k * chunk;
+    tr.s1 = min(tr.ray.hi, tr.s0 + chunk);
+}
+
+__device__ __forceinline__ void setup_thread_ray(const MarchParams& p, const float (&m)[12], int b, int n, int k,
+                                                 ThreadRay& tr) {
+    init_thread_ray(p, m, b, n, tr);
+    chunk_thread_ray(tr, k, p.K);
+}
+
+// Narrow the box-culled window of a ray with the occupancy grid.
+//  NDRR_SKIP_OCCUPANCY: march the distance field from both ends of the window
+//  to the first occupied cell; every sample outside [t_near, t_far] lies in an
+//  empty cell. NDRR_SKIP_PROPOSAL: keep the proposed [pn, pf] only if the
+//  distance field shows both outer segments empty, else keep the full window
+//  (a fallback). Returns true when the ray fell back.
+__device__ __forceinline__ bool apply_skip(const MarchParams& p, ThreadRay& tr, float pn, float pf) {
+    Ray& r = tr.ray;
+    if (tr.n < 0 || r.lo >= r.hi) return false;
+    const float sm1 = (float)(p.S - 1);
+    const float tb0 = (float)r.lo * p.inv_s, tb1 = (float)(r.hi - 1) * p.inv_s;
+    float tn, tf;
+    if (p.skip_mode == NDRR_SKIP_OCCUPANCY) {
+        const int h1 = first_occupied(p.occ, r, tb0, tb1, kSkipSteps, &tn);
+        if (h1 == 0) {
+            r.hi = r.lo;  // nothing occupied along the window
+            return false;
+        }
+        if (h1 < 0) return true;
+        const int h2 = first_occupied(p.occ, r, tb1, tn, kSkipSteps, &tf);
+        if (h2 != 1) tf = tb1;
+    } else {
+        tn = pn - p.margin * p.inv_s;
+        tf = pf + p.margin * p.inv_s;
+        float unused;
+        if (first_occupied(p.occ, r, tb0, fminf(tn, tb1), kSkipSteps, &unused) != 0) return true;
+        if (first_occupied(p.occ, r, tb1, fmaxf(tf, tb0), kSkipSteps, &unused) != 0) return true;
+        if (tn > tf) {
+            r.hi = r.lo;
+            return false;
+        }
+    }
+    // Keep one extra sample on each side of [tn, tf].
+    const float a = fminf(fmaxf(floorf(tn * sm1) - 1.0f, (float)r.lo), (float)r.hi);
+    const float e = fminf(fmaxf(ceilf(tf * sm1) + 2.0f, (float)r.lo), (float)r.hi);
+    r.lo = (int)a;
+    r.hi = max((int)e, r.lo);
+    return false;
+}
+
+// Accumulate the CTA's skip counters into p.stats (one atomic per counter).
+__device__ __forceinline__ void skip_stats_add(const MarchParams& p, unsigned long long* sstat, int k, bool has,
+                                               bool fell, int box_len, int len) {
+    if (k == 0) {
+        unsigned v0 = __ballot_sync(0xffffffffu, has), v1 = __ballot_sync(0xffffffffu, fell);
+        unsigned long long l = (unsigned long long)len, bl = (unsigned long long)box_len;
+        for (int o = 16; o > 0; o >>= 1) {
+            l += __shfl_xor_sync(0xffffffffu, l, o);
+            bl += __shfl_xor_sync(0xffffffffu, bl, o);
+        }
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(sstat + 0, (unsigned long long)__popc(v0));
+            atomicAdd(sstat + 1, (unsigned long long)__popc(v1));
+            atomicAdd(sstat + 2, l);
+            atomicAdd(sstat + 3, bl);
+        }
+    }
+}
+
+// ===================================================================== forward
+// SKIP: 0 no skipping, 1 occupancy window, 2 learned proposal + check.
+template <typename VT, typename OT, bool MULTI, int SKIP>
+__device__ __forceinline__ void fwd_body(const MarchParams& p) {
+    extern __shared__ float smem[];
+    const int R = p.tw * p.th;
+    const int NT = R * p.K;
+    const int tid = threadIdx.x;
+    const int r = tid % R, k = tid / R;
+    const int tile = blockIdx.x % p.tm.tiles;
+    const int b = blockIdx.x / p.tm.tiles;
+    const int n = tile_ray(p.tm, p.N, p.tw, p.th, tile, r);
+
+    float m[12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) m[j] = __ldg(p.M + (size_t)b * 12 + j);
+
+    ThreadRay tr;
+    init_thread_ray(p, m, b, n, tr);
+    if (SKIP != 0) {
+        const int box_len = max(tr.ray.hi - tr.ray.lo, 0);
+        const bool has = n >= 0 && box_len > 0;
+        float pn = 0.f, pf = 1.f;
+        if (SKIP == 2)
+            proposal_window_cta(p.proposal, reinterpret_cast<unsigned char*>(smem) + p.prop_off, tr.ray, p.D, p.H,
+                                p.W, has, r, k, R, pn, pf);
+        const bool fell = apply_skip(p, tr, pn, pf);
+        if (p.stats) skip_stats_add(p, p.stats, k, has, fell, box_len, max(tr.ray.hi - tr.ray.lo, 0));
+    }
+    chunk_thread_ray(tr, k, p.K);
+
+    const VT* __restrict__ vol = reinterpret_cast<const VT*>(p.vol);
+    float acc = 0.f;
+    int first = INT_MAX, last = -1;  // non-empty extent of this thread's chunk
+    float* cacc = smem + tid;  // MULTI: per-thread class accumulators, stride NT
+    if (MULTI) {
+        for (int c = 0; c < p.C; ++c) cacc[c * NT] = 0.f;
+    }
+    for (int s = tr.s0; s < tr.s1; ++s) {
+        const float t = (float)s * p.inv_s;
+        const float x = fmaf(t, tr.ray.dx, tr.ray.p0x);
+        const float y = fmaf(t, tr.ray.dy, tr.ray.p0y);
+        const float z = fmaf(t, tr.ray.dz, tr.ray.p0z);
+        Cell cell;
+        load_cell(vol, p.D, p.H, p.W, x, y, z, cell);
+        const float val = cell_value(cell);
+        acc += val;
+        if (p.out_extent) {
+            const bool nz = (cell.v000 != 0.f) | (cell.v001 != 0.f) | (cell.v010 != 0.f) | (cell.v011 != 0.f) |
+                            (cell.v100 != 0.f) | (cell.v101 != 0.f) | (cell.v110 != 0.f) | (cell.v111 != 0.f);
+            if (nz) {
+                first = min(first, s);
+                last = s;
+            }
+        }
+        if (MULTI) {
+            const int cls = nearest_label(p.lab, p.lab_dtype, p.D, p.H, p.W, x, y, z);
+            if ((unsigned)cls < (unsigned)p.C) cacc[cls * NT] += val;
+        }
+    }
+
+    // Sum the K chunk partials of each ray in a fixed order.
+    float* red = smem + (MULTI ? (size_t)p.C * NT : 0);
+    red[tid] = acc;
+    if (p.out_extent) {
+        // Non-empty extent across the K chunks (stored after the partials).
+        int* ext = reinterpret_cast<int*>(red + NT);
+        ext[tid] = first;
+        ext[NT + tid] = last;
+    }
+    __syncthreads();
+    if (p.out_extent && k == 0 && n >= 0) {
+        const int* ext = reinterpret_cast<const int*>(red + NT);
+        int f = ext[r], l = ext[NT + r];
+        for (int j = 1; j < p.K; ++j) {
+            f = min(f, ext[r + j * R]);
+            l = max(l, ext[NT + r + j * R]);
+        }
+        const bool any = l >= 0;
+        p.out_extent[tr.bn * 2 + 0] = any ? (float)f * p.inv_s : 1.f;
+        p.out_extent[tr.bn * 2 + 1] = any ? (float)l * p.inv_s : 0.f;
+    }
+    OT* out = reinterpret_cast<OT*>(p.out);
+    OT* out_total = reinterpret_cast<OT*>(p.out_total);
+    if (!MULTI) {
+        if (k == 0 && n >= 0) {
+            float sum = red[r];
+            for (int j = 1; j < p.K; ++j) sum += red[r + j * R];
+            st_out(out, tr.bn, sum * tr.stepv);
+            if (out_total) st_out(out_total, tr.bn, sum * tr.stepv);
+        }
+    } else {
+        if (out_total && k == 0 && n >= 0) {
+            float sum = red[r];
+            for (int j = 1; j < p.K; ++j) sum += red[r + j * R];
+            st_out(out_total, tr.bn, sum * tr.stepv);
+        }
+        // Channel write-out: consecutive threads take consecutive rays of one
+        // channel, so stores coalesce along the detector rows.
+        for (int idx = tid; idx < R * p.C; idx += NT) {
+            const int rr = idx % R, c = idx / R;
+            const int nn = tile_ray(p.tm, p.N, p.tw, p.th, tile, rr);
+            if (nn < 0) continue;
+            float sum = smem[(size_t)c * NT + rr];
+            for (int j = 1; j < p.K; ++j) sum += smem[(size_t)c * NT + rr + j * R];
+            const size_t bn = (size_t)b * p.N + nn;
+            st_out(out, ((size_t)b * p.C + c) * p.N + nn, sum * __ldg(p.step + bn));
+        }
+    }
+}
+
+template <typename VT, typename OT, bool MULTI, int SKIP>
+__global__ void __launch_bounds__(512, 2) raymarch_fwd_kernel(const MarchParams p) {
+    fwd_body<VT, OT, MULTI, SKIP>(p);
+}
+
+// Proposal mode: the tensor-core inference prologue needs more registers.
+template <typename VT, typename OT, bool MULTI>
+__global__ void __launch_bounds__(256, 3) raymarch_fwd_prop_kernel(const MarchParams p) {
+    fwd_body<VT, OT, MULTI, 2>(p);
+}
+
+// ===================================================================== adjoint
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Per-thread adjoint accumulators.
+struct AdjAcc {
+    float a[12];  // dL/dM partial (row-major 3 x 4)
+    float gsx, gsy, gsz, gtx, gty, gtz, gst;
+    __device__ __forceinline__ void zero() {
+#pragma unroll
+        for (int j = 0; j < 12; ++j) a[j] = 0.f;
+        gsx = gsy = gsz = gtx = gty = gtz = gst = 0.f;
+    }
+};
+
+// Volume-gradient scatter straight to global memory: one atomic per tap.
+struct DirectScatter {
+    float* __restrict__ gvol;
+    int D, H, W;
+    __device__ __forceinline__ void operator()(int idx_unused, int ix, int iy, int iz, float g00, float g01,
+                                               float g10, float g11, float wx0, float wx1) const {
+        (void)idx_unused;
+        const int HW = H * W;
+        const int base = (iz * H + iy) * W + ix;
+        if ((unsigned)ix < (unsigned)(W - 1) && (unsigned)iy < (unsigned)(H - 1) && (unsigned)iz < (unsigned)(D - 1)) {
+            atomicAdd(gvol + base, g00 * wx0);
+            atomicAdd(gvol + base + 1, g00 * wx1);
+            atomicAdd(gvol + base + W, g01 * wx0);
+            atomicAdd(gvol + base + W + 1, g01 * wx1);
+            atomicAdd(gvol + base + HW, g10 * wx0);
+            atomicAdd(gvol + base + HW + 1, g10 * wx1);
+            atomicAdd(gvol + base + HW + W, g11 * wx0);
+            atomicAdd(gvol + base + HW + W + 1, g11 * wx1);
+        } else {
+            const bool x0 = (unsigned)ix < (unsigned)W, x1 = (unsigned)(ix + 1) < (unsigned)W;
+            const bool y0 = (unsigned)iy < (unsigned)H, y1 = (unsigned)(iy + 1) < (unsigned)H;
+            const bool z0 = (unsigned)iz < (unsigned)D, z1 = (unsigned)(iz + 1) < (unsigned)D;
+            if (z0 && y0 && x0) atomicAdd(gvol + base, g00 * wx0);
+            if (z0 && y0 && x1) atomicAdd(gvol + base + 1, g00 * wx1);
+            if (z0 && y1 && x0) atomicAdd(gvol + base + W, g01 * wx0);
+            if (z0 && y1 && x1) atomicAdd(gvol + base + W + 1, g01 * wx1);
+            if (z1 && y0 && x0) atomicAdd(gvol + base + HW, g10 * wx0);
+            if (z1 && y0 && x1) atomicAdd(gvol + base + HW + 1, g10 * wx1);
+            if (z1 && y1 && x0) atomicAdd(gvol + base + HW + W, g11 * wx0);
+            if (z1 && y1 && x1) atomicAdd(gvol + base + HW + W + 1, g11 * wx1);
+        }
+    }
+};
+
+// Volume-gradient scatter into a shared-memory brick covering the box
+// [x0, x0 + nx) x [y0, y0 + ny) x [z0, z0 + nz), which contains every
+// in-volume corner the current slab can touch (shared-memory atomics).
+struct BrickScatter {
+    float* acc;
+    int D, H, W;
+    int x0, y0, z0, nx, ny;
+    __device__ __forceinline__ void operator()(int, int ix, int iy, int iz, float g00, float g01, float g10,
+                                               float g11, float wx0, float wx1) const {
+        const int lx = ix - x0, ly = iy - y0, lz = iz - z0;
+        const int nxy = nx * ny;
+        const int base = (lz * ny + ly) * nx + lx;
+        const bool x0ok = (unsigned)ix < (unsigned)W, x1ok = (unsigned)(ix + 1) < (unsigned)W;
+        const bool y0ok = (unsigned)iy < (unsigned)H, y1ok = (unsigned)(iy + 1) < (unsigned)H;
+        const bool z0ok = (unsigned)iz < (unsigned)D, z1ok = (unsigned)(iz + 1) < (unsigned)D;
+        if (z0ok && y0ok && x0ok) atomicAdd(acc + base, g00 * wx0);
+        if (z0ok && y0ok && x1ok) atomicAdd(acc + base + 1, g00 * wx1);
+        if (z0ok && y1ok && x0ok) atomicAdd(acc + base + nx, g01 * wx0);
+        if (z0ok && y1ok && x1ok) atomicAdd(acc + base + nx + 1, g01 * wx1);
+        if (z1ok && y0ok && x0ok) atomicAdd(acc + base + nxy, g10 * wx0);
+        if (z1ok && y0ok && x1ok) atomicAdd(acc + base + nxy + 1, g10 * wx1);
+        if (z1ok && y1ok && x0ok) atomicAdd(acc + base + nxy + nx, g11 * wx0);
+        if (z1ok && y1ok && x1ok) atomicAdd(acc + base + nxy + nx + 1, g11 * wx1);
+    }
+};
+
+// Adjoint of samples [s0, s1) of one ray (reference _fused.py:230-298).
+template <typename VT, bool MULTI, bool GVOL, bool GCAM, typename Scatter>
+__device__ __forceinline__ void adjoint_samples(const MarchParams& p, const float (&m)[12], const ThreadRay& tr,
+                                                int b, int s0, int s1, float go_ray, AdjAcc& A,
+                                                const Scatter& scatter) {
+    const VT* __restrict__ vol = reinterpret_cast<const VT*>(p.vol);
+    for (int s = s0; s < s1; ++s) {
+        const float t = (float)s * p.inv_s;
+        const float x = fmaf(t, tr.ray.dx, tr.ray.p0x);
+        const float y = fmaf(t, tr.ray.dy, tr.ray.p0y);
+        const float z = fmaf(t, tr.ray.dz, tr.ray.p0z);
+        float gg = go_ray;
+        if (MULTI) {
+            // Upstream gradient of this sample's channel; out-of-range labels
+            // are masked like the forward drops them (_fused.py:233-237).
+            const int cls = nearest_label(p.lab, p.lab_dtype, p.D, p.H, p.W, x, y, z);
+            gg = ((unsigned)cls < (unsigned)p.C) ? ld_any_f(p.go, p.go_dtype, ((size_t)b * p.C + cls) * p.N + tr.n)
+                                                 : 0.f;
+        }
+        // Every adjoint term of this sample is proportional to gg.
+        if (gg == 0.f) continue;
+        const float g = gg * tr.stepv;
+        Cell cell;
+        load_cell(vol, p.D, p.H, p.W, x, y, z, cell);
+        float dvx, dvy, dvz;
+        cell_grad(cell, dvx, dvy, dvz);
+        const float gx = g * dvx, gy = g * dvy, gz = g * dvz;
+        const float qx = fmaf(t, tr.ex, tr.sx), qy = fmaf(t, tr.ey, tr.sy), qz = fmaf(t, tr.ez, tr.sz);
+        A.a[0] = fmaf(gx, qx, A.a[0]);
+        A.a[1] = fmaf(gx, qy, A.a[1]);
+        A.a[2] = fmaf(gx, qz, A.a[2]);
+        A.a[3] += gx;
+        A.a[4] = fmaf(gy, qx, A.a[4]);
+        A.a[5] = fmaf(gy, qy, A.a[5]);
+        A.a[6] = fmaf(gy, qz, A.a[6]);
+        A.a[7] += gy;
+        A.a[8] = fmaf(gz, qx, A.a[8]);
+        A.a[9] = fmaf(gz, qy, A.a[9]);
+        A.a[10] = fmaf(gz, qz, A.a[10]);
+        A.a[11] += gz;
+        if (GCAM) {
+            // Chain to camera space: gq = M[:, :3]^T gpos.
+            const float gqx = m[0] * gx + m[4] * gy + m[8] * gz;
+            const float gqy = m[1] * gx + m[5] * gy + m[9] * gz;
+            const float gqz = m[2] * gx + m[6] * gy + m[10] * gz;
+            const float omt = 1.f - t;
+            A.gsx = fmaf(omt, gqx, A.gsx);
+            A.gsy = fmaf(omt, gqy, A.gsy);
+            A.gsz = fmaf(omt, gqz, A.gsz);
+            A.gtx = fmaf(t, gqx, A.gtx);
+            A.gty = fmaf(t, gqy, A.gty);
+            A.gtz = fmaf(t, gqz, A.gtz);
+            A.gst = fmaf(gg, cell_value(cell), A.gst);
+        }
+        if (GVOL) {
+            const float wy0 = 1.f - cell.fy, wz0 = 1.f - cell.fz;
+            scatter(0, cell.ix, cell.iy, cell.iz, g * wz0 * wy0, g * wz0 * cell.fy, g * cell.fz * wy0,
+                    g * cell.fz * cell.fy, 1.f - cell.fx, cell.fx);
+        }
+    }
+}
+
+// CTA epilogue shared by the adjoint kernels: fixed-order reduction of the
+// pose partials into `partials[blockIdx.x]`, and the per-ray camera
+// gradients (summing the K sample chunks of each ray in order).
+template <bool GCAM>
+__device__ __forceinline__ void adjoint_epilogue(const MarchParams& p, const ThreadRay& tr, const AdjAcc& A,
+                                                 float* smem, int R, int NT, int r, int k) {
+    const int tid = threadIdx.x;
+    const bool shared_src = GCAM && !p.src_per_ray;
+    const int nwarps = NT >> 5;
+    const int warp = tid >> 5, lane = tid & 31;
+    float* wred = smem;  // [nwarps][kPartialStride]
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < 12; ++j) {
+        const float v = warp_sum(A.a[j]);
+        if (lane == 0) wred[warp * kPartialStride + j] = v;
+    }
+    if (shared_src) {
+        const float v0 = warp_sum(A.gsx), v1 = warp_sum(A.gsy), v2 = warp_sum(A.gsz);
+        if (lane == 0) {
+            wred[warp * kPartialStride + 12] = v0;
+            wred[warp * kPartialStride + 13] = v1;
+            wred[warp * kPartialStride + 14] = v2;
+        }
+    }
+    __syncthreads();
+    const int nterms = shared_src ? 15 : 12;
+    if (tid < nterms) {
+        float sum = wred[tid];
+        for (int w = 1; w < nwarps; ++w) sum += wred[w * kPartialStride + tid];
+        p.partials[(size_t)blockIdx.x * kPartialStride + tid] = sum;
+    }
+    if (GCAM) {
+        __syncthreads();
+        float* cr = smem;  // [7][NT]
+        cr[0 * NT + tid] = A.gtx;
+        cr[1 * NT + tid] = A.gty;
+        cr[2 * NT + tid] = A.gtz;
+        cr[3 * NT + tid] = A.gst;
+        cr[4 * NT + tid] = A.gsx;
+        cr[5 * NT + tid] = A.gsy;
+        cr[6 * NT + tid] = A.gsz;
+        __syncthreads();
+        if (k == 0 && tr.n >= 0) {
+            float v[7];
+#pragma unroll
+            for (int q = 0; q < 7; ++q) {
+                float sum = cr[q * NT + r];
+                for (int j = 1; j < p.K; ++j) sum += cr[q * NT + r + j * R];
+                v[q] = sum;
+            }
+            p.gtgt[tr.bn * 3 + 0] = v[0];
+            p.gtgt[tr.bn * 3 + 1] = v[1];
+            p.gtgt[tr.bn * 3 + 2] = v[2];
+            p.gstep[tr.bn] = v[3];
+            if (p.src_per_ray) {
+                p.gsrc[tr.bn * 3 + 0] = v[4];
+                p.gsrc[tr.bn * 3 + 1] = v[5];
+                p.gsrc[tr.bn * 3 + 2] = v[6];
+            }
+        }
+    }
+}
+
+// Adjoint with direct global atomics for the volume gradient.
+// SKIP (only with GVOL false, see apply_skip): 0, 1 occupancy, 2 proposal.
+template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP>
+__device__ __forceinline__ void bwd_body(const MarchParams& p) {
+    extern __shared__ float smem[];
+    const int R = p.tw * p.th;
+    const int NT = R * p.K;
+    const int tid = threadIdx.x;
+    const int r = tid % R, k = tid / R;
+    const int tile = blockIdx.x % p.tm.tiles;
+    const int b = blockIdx.x / p.tm.tiles;
+    const int n = tile_ray(p.tm, p.N, p.tw, p.th, tile, r);
+
+    float m[12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) m[j] = __ldg(p.M + (size_t)b * 12 + j);
+    ThreadRay tr;
+    init_thread_ray(p, m, b, n, tr);
+    if (!GVOL && SKIP != 0) {
+        // Skipped samples have eight zero corners: no pose or camera terms.
+        const bool has = n >= 0 && tr.ray.hi > tr.ray.lo;
+        float pn = 0.f, pf = 1.f;
+        if (SKIP == 2)
+            proposal_window_cta(p.proposal, reinterpret_cast<unsigned char*>(smem) + p.prop_off, tr.ray, p.D, p.H,
+                                p.W, has, r, k, R, pn, pf);
+        apply_skip(p, tr, pn, pf);
+    }
+    chunk_thread_ray(tr, k, p.K);
+    float go_ray = 0.f;
+    if (!MULTI && n >= 0) go_ray = ld_any_f(p.go, p.go_dtype, tr.bn);
+
+    AdjAcc A;
+    A.zero();
+    const DirectScatter sc{p.gvol, p.D, p.H, p.W};
+    adjoint_samples<VT, MULTI, GVOL, GCAM>(p, m, tr, b, tr.s0, tr.s1, go_ray, A, sc);
+    adjoint_epilogue<GCAM>(p, tr, A, smem, R, NT, r, k);
+}
+
+template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP>
+__global__ void __launch_bounds__(512, 1) raymarch_bwd_kernel(const MarchParams p) {
+    bwd_body<VT, MULTI, GVOL, GCAM, SKIP>(p);
+}
+
+template <typename VT, bool MULTI, bool GCAM>
+__global__ void __launch_bounds__(256, 3) raymarch_bwd_prop_kernel(const MarchParams p) {
+    bwd_body<VT, MULTI, false, GCAM, 2>(p);
+}
+
+// Block-wide min of (a0..a2, -b0..-b2): the union box of per-thread boxes.
+// `sred` holds nwarps * 6 ints; the result lands in box[0..5] for every thread.
+__device__ __forceinline__ void block_box(int (&lo)[3], int (&hi)[3], int* sred, int* box, int nwarps) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int v[6] = {lo[0], lo[1], lo[2], -hi[0], -hi[1], -hi[2]};
+#pragma unroll
+    for (int j = 0; j < 6; ++j) v[j] = __reduce_min_sync(0xffffffffu, v[j]);
+    if (lane == 0) {
+#pragma unroll
+        for (int j = 0; j < 6; ++j) sred[warp * 6 + j] = v[j];
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        int m = sred[threadIdx.x];
+        for (int w = 1; w < nwarps; ++w) m = min(m, sred[w * 6 + threadIdx.x]);
+        box[threadIdx.x] = m;
+    }
+    __syncthreads();
+    lo[0] = box[0];
+    lo[1] = box[1];
+    lo[2] = box[2];
+    hi[0] = -box[3];
+    hi[1] = -box[4];
+    hi[2] = -box[5];
+}
+
+__device__ __forceinline__ int floor_clamped(float v, float lo, float hi) {
+    return (int)floorf(fminf(fmaxf(v, lo), hi));
+}
+
+// Adjoint with the volume gradient privatised per slab: the CTA's rays march
+// in lockstep over sample slabs [sb, sb + L); for each slab the union of the
+// rays' cell boxes (exact: positions are monotone in s, so the two slab ends
+// bound every sample) is accumulated in shared memory and flushed to global
+// memory with one coalesced atomic per touched voxel. Slabs whose box exceeds
+// `cap` voxels fall back to direct atomics, and L adapts to keep boxes small.
+// One thread per ray (sample_split = 1).
+template <typename VT, bool MULTI, bool GCAM>
+__global__ void __launch_bounds__(256, 2) raymarch_bwd_brick_kernel(const MarchParams p, int cap, int L0) {
+    extern __shared__ float smem[];
+    const int R = p.tw * p.th;
+    const int NT = R;
+    const int nwarps = NT >> 5;
+    const int tid = threadIdx.x;
+    const int tile = blockIdx.x % p.tm.tiles;
+    const int b = blockIdx.x / p.tm.tiles;
+    const int n = tile_ray(p.tm, p.N, p.tw, p.th, tile, tid);
+    float* acc = smem;                                   // [cap] brick
+    int* sred = reinterpret_cast<int*>(smem + cap);      // [nwarps * 6]
+    int* box = sred + nwarps * 6;                        // [8]
+
+    float m[12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) m[j] = __ldg(p.M + (size_t)b * 12 + j);
+    ThreadRay tr;
+    setup_thread_ray(p, m, b, n, 0, tr);
+    float go_ray = 0.f;
+    if (!MULTI && n >= 0) go_ray = ld_any_f(p.go, p.go_dtype, tr.bn);
+
+    // Tile-wide sample range. Empty entries use (INT_MAX, -INT_MAX) so that
+    // the negation inside block_box cannot overflow.
+    int lo3[3], hi3[3];
+    {
+        const bool any = tr.s0 < tr.s1;
+        lo3[0] = any ? tr.s0 : INT_MAX;
+        hi3[0] = any ? tr.s1 : -INT_MAX;
+        lo3[1] = lo3[2] = INT_MAX;
+        hi3[1] = hi3[2] = -INT_MAX;
+        block_box(lo3, hi3, sred, box, nwarps);
+    }
+    const int smin = lo3[0], smax = hi3[0];
+
+    AdjAcc A;
+    A.zero();
+    const float fW = (float)p.W, fH = (float)p.H, fD = (float)p.D;
+    int L = L0;
+    for (int sb = smin; sb < smax;) {
+        const int se = min(sb + L, smax);
+        const int a = max(tr.s0, sb), e = min(tr.s1, se);
+        lo3[0] = lo3[1] = lo3[2] = INT_MAX;
+        hi3[0] = hi3[1] = hi3[2] = -INT_MAX;
+        if (a < e) {
+            const float ta = (float)a * p.inv_s, te = (float)(e - 1) * p.inv_s;
+            const int xa = floor_clamped(fmaf(ta, tr.ray.dx, tr.ray.p0x), -2.f, fW + 1.f);
+            const int xe = floor_clamped(fmaf(te, tr.ray.dx, tr.ray.p0x), -2.f, fW + 1.f);
+            const int ya = floor_clamped(fmaf(ta, tr.ray.dy, tr.ray.p0y), -2.f, fH + 1.f);
+            const int ye = floor_clamped(fmaf(te, tr.ray.dy, tr.ray.p0y), -2.f, fH + 1.f);
+            const int za = floor_clamped(fmaf(ta, tr.ray.dz, tr.ray.p0z), -2.f, fD + 1.f);
+            const int ze = floor_clamped(fmaf(te, tr.ray.dz, tr.ray.p0z), -2.f, fD + 1.f);
+            // corners span [floor, floor + 1], clipped to the volume
+            int l0 = max(min(xa, xe), 0), h0 = min(max(xa, xe) + 1, p.W - 1);
+            int l1 = max(min(ya, ye), 0), h1 = min(max(ya, ye) + 1, p.H - 1);
+            int l2 = max(min(za, ze), 0), h2 = min(max(za, ze) + 1, p.D - 1);
+            if (l0 <= h0 && l1 <= h1 && l2 <= h2) {
+                lo3[0] = l0; lo3[1] = l1; lo3[2] = l2;
+                hi3[0] = h0; hi3[1] = h1; hi3[2] = h2;
+            }
+        }
+        block_box(lo3, hi3, sred, box, nwarps);
+        const bool empty = lo3[0] > hi3[0];
+        const int nx = empty ? 0 : hi3[0] - lo3[0] + 1;
+        const int ny = empty ? 0 : hi3[1] - lo3[1] + 1;
+        const int nz = empty ? 0 : hi3[2] - lo3[2] + 1;
+        const long long nvox = (long long)nx * ny * nz;
+        const bool use_brick = nvox > 0 && nvox <= cap;
+        if (use_brick) {
+            float4* a4 = reinterpret_cast<float4*>(acc);
+            const int n4 = (int)(nvox >> 2);
+            for (int i = tid; i < n4; i += NT) a4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int i = (n4 << 2) + tid; i < (int)nvox; i += NT) acc[i] = 0.f;
+            __syncthreads();
+            const BrickScatter sc{acc, p.D, p.H, p.W, lo3[0], lo3[1], lo3[2], nx, ny};
+            adjoint_samples<VT, MULTI, true, GCAM>(p, m, tr, b, a, e, go_ray, A, sc);
+            __syncthreads();
+            // Flush: each warp takes whole rows so lanes write consecutive x.
+            const int warp = tid >> 5, lane = tid & 31;
+            const int rows = ny * nz;
+            for (int row = warp; row < rows; row += nwarps) {
+                const int ly = row % ny, lz = row / ny;
+                float* g = p.gvol + ((size_t)(lo3[2] + lz) * p.H + (lo3[1] + ly)) * p.W + lo3[0];
+                const float* s = acc + row * nx;
+                for (int lx = lane; lx < nx; lx += 32) {
+                    const float v = s[lx];
+                    if (v != 0.f) atomicAdd(g + lx, v);
+                }
+            }
+            if (nvox * 4 < cap) L = min(L * 2, 256);
+        } else {
+            const DirectScatter sc{p.gvol, p.D, p.H, p.W};
+            adjoint_samples<VT, MULTI, true, GCAM>(p, m, tr, b, a, e, go_ray, A, sc);
+            if (nvox > cap) L = max(L >> 1, 2);
+        }
+        sb = se;
+    }
+    adjoint_epilogue<GCAM>(p, tr, A, smem, R, NT, tid, 0);
+}
+
+// Per-pose sum of the per-tile partials in a fixed order. One CTA per pose.
+cudaError_t launch_brick(const ndrr_raymarch_args& a, const LaunchShape& ls, const MarchParams& p, unsigned grid,
+                         unsigned block, cudaStream_t st);
+
+MarchParams make_params(const ndrr_raymarch_args& a, const LaunchShape& ls);
+size_t fwd_base_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
+
+template <typename Kern>
+static cudaError_t launch_kernel(Kern kern, unsigned grid, unsigned block, size_t smem, cudaStream_t st,
+                                 const MarchParams& p) {
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    kern<<<grid, block, smem, st>>>(p);
+    return cudaGetLastError();
+}
+
+}  // namespace ndrr

@@ -103,6 +103,22 @@ def _base_args(vol, lab, M, src, tgt, step, n_samples, n_classes, width) -> _ffi
     return a
 
 
+def _apply_skip(a: _ffi.RaymarchArgs, skip, vol: torch.Tensor) -> None:
+    """Fill the empty-space fields of the C-ABI arguments from an EmptySpace."""
+    if skip is None or skip.mode == _ffi.NDRR_SKIP_NONE:
+        return
+    g = skip.grid
+    if g.grid.device != vol.device or tuple(g.volume_shape) != tuple(vol.shape):
+        raise ValueError("the occupancy grid was built for another volume or device")
+    a.skip_mode = int(skip.mode)
+    a.occ_cell = g.cell
+    a.occ_gz, a.occ_gy, a.occ_gx = g.grid.shape
+    a.occ_grid = g.grid.data_ptr()
+    a.proposal_margin = float(skip.margin)
+    if skip.mode == _ffi.NDRR_SKIP_PROPOSAL:
+        a.proposal_params = skip.packed.data_ptr()
+
+
 def _prep(vol, lab, M, src, tgt, step):
     vol = vol.contiguous()
     lab = lab.contiguous()
@@ -126,8 +142,17 @@ def raymarch_forward(
     t_window: torch.Tensor | None = None,
     with_total: bool = False,
     out_dtype: torch.dtype | None = None,
+    tile: tuple[int, int, int] | None = None,
+    skip=None,
+    extent: torch.Tensor | None = None,
+    stats: torch.Tensor | None = None,
 ) -> tuple[torch.Tensor, torch.Tensor | None]:
-    """Launch the forward kernel; returns (out [B, C, N], total [B, N] or None)."""
+    """Launch the forward kernel; returns (out [B, C, N], total [B, N] or None).
+
+    `tile` optionally fixes the launch shape (tile_w, tile_h, sample_split).
+    `skip` is an `EmptySpace` (empty-space skipping), `extent` an optional
+    float32 [B, N, 2] output receiving each ray's non-empty interval in t,
+    `stats` an optional int64 [4] counter tensor (see ndrr_raymarch_args)."""
     _check_inputs(vol, lab, M, src, tgt, step, n_samples, n_classes)
     vol, lab, M, src, tgt, step = _prep(vol, lab, M, src, tgt, step)
     B, N, _ = tgt.shape
@@ -143,6 +168,17 @@ def raymarch_forward(
         if t_window.shape != (B, N, 2):
             raise ValueError(f"t_window must be [B, N, 2], got {tuple(t_window.shape)}")
         a.t_window = _ptr(t_window)
+    if tile is not None:
+        a.tile_w, a.tile_h, a.sample_split = (int(v) for v in tile)
+    _apply_skip(a, skip, vol)
+    if extent is not None:
+        if extent.shape != (B, N, 2) or extent.dtype != torch.float32 or not extent.is_contiguous():
+            raise ValueError("extent must be a contiguous float32 [B, N, 2] tensor")
+        a.out_extent = extent.data_ptr()
+    if stats is not None:
+        if stats.dtype != torch.int64 or stats.numel() < 4 or not stats.is_contiguous():
+            raise ValueError("stats must be a contiguous int64 tensor with 4 entries")
+        a.skip_stats = stats.data_ptr()
     lib = _ffi.load()
     _ffi.check(lib.ndrr_raymarch_fwd(ctypes.byref(a), _stream_handle(vol.device)), "ndrr_raymarch_fwd")
     return out, total
@@ -163,12 +199,19 @@ def raymarch_backward(
     need_gcam: bool,
     t_window: torch.Tensor | None = None,
     gvol: torch.Tensor | None = None,
+    gvol_mode: int = 0,
+    brick_cap: int = 0,
+    tile: tuple[int, int, int] | None = None,
+    skip=None,
 ):
     """Launch the adjoint; returns (gvol, gM, gsrc, gtgt, gstep) in float32.
 
     `gvol`, when given, is a float32 [D, H, W] buffer the volume gradient is
     accumulated into (so several calls can share one); otherwise a zeroed one
-    is allocated."""
+    is allocated. `gvol_mode` selects the volume-gradient scatter (0 auto,
+    1 direct atomics, 2 per-slab shared-memory brick), `brick_cap` the brick
+    capacity in voxels (0 = default) and `tile` an explicit
+    (tile_w, tile_h, sample_split) launch shape."""
     _check_inputs(vol, lab, M, src, tgt, step, n_samples, n_classes)
     vol, lab, M, src, tgt, step = _prep(vol, lab, M, src, tgt, step)
     B, N, _ = tgt.shape
@@ -205,6 +248,11 @@ def raymarch_backward(
     if t_window is not None:
         t_window = t_window.float().contiguous()
         a.t_window = _ptr(t_window)
+    a.gvol_mode = int(gvol_mode)
+    a.reserved[0] = int(brick_cap)
+    _apply_skip(a, skip, vol)
+    if tile is not None:
+        a.tile_w, a.tile_h, a.sample_split = (int(v) for v in tile)
     lib = _ffi.load()
     nbytes = ctypes.c_uint64(0)
     _ffi.check(lib.ndrr_raymarch_bwd_workspace_bytes(ctypes.byref(a), ctypes.byref(nbytes)), "workspace query")
@@ -307,3 +355,122 @@ def _backward(ctx, go):
 
 
 torch.library.register_autograd("nanodrr_gb300::fused_raymarch", _backward, setup_context=_setup_context)
+
+
+# ------------------------------------------------ empty-space-skipping op
+# Same contract as fused_raymarch plus the skip structures: an occupancy grid
+# (uint8 [gz, gy, gx]), its cell size, the packed proposal parameters (uint8,
+# empty for the occupancy mode), the mode and the interval margin. Skipped
+# samples have eight zero corners, so the output and the pose/camera
+# gradients equal the plain march's; the volume gradient is computed over the
+# full box-culled window.
+class _SkipArgs:
+    def __init__(self, grid, cell, packed, mode, margin, shape):
+        from .empty_space import OccupancyGrid
+
+        self.grid = OccupancyGrid(grid, cell, shape)
+        self.packed = packed
+        self.mode = mode
+        self.margin = margin
+
+
+@torch.library.custom_op("nanodrr_gb300::fused_raymarch_skip", mutates_args=())
+def fused_raymarch_skip(
+    vol: torch.Tensor,
+    lab: torch.Tensor,
+    M: torch.Tensor,
+    src: torch.Tensor,
+    tgt: torch.Tensor,
+    step: torch.Tensor,
+    n_samples: int,
+    n_classes: int,
+    width: int,
+    occ_grid: torch.Tensor,
+    occ_cell: int,
+    proposal: torch.Tensor,
+    skip_mode: int,
+    margin: float,
+) -> torch.Tensor:
+    skip = _SkipArgs(occ_grid, occ_cell, proposal, skip_mode, margin, vol.shape)
+    out, _ = raymarch_forward(vol, lab, M, src, tgt, step, n_samples, n_classes, width, skip=skip)
+    return out
+
+
+@fused_raymarch_skip.register_fake
+def _(vol, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell, proposal, skip_mode, margin):
+    B, N, _ = tgt.shape
+    return torch.empty(B, n_classes, N, device=vol.device, dtype=vol.dtype)
+
+
+@torch.library.custom_op("nanodrr_gb300::fused_raymarch_skip_bwd", mutates_args=())
+def fused_raymarch_skip_bwd(
+    go: torch.Tensor,
+    vol: torch.Tensor,
+    lab: torch.Tensor,
+    M: torch.Tensor,
+    src: torch.Tensor,
+    tgt: torch.Tensor,
+    step: torch.Tensor,
+    n_samples: int,
+    n_classes: int,
+    width: int,
+    need_gvol: bool,
+    need_gcam: bool,
+    occ_grid: torch.Tensor,
+    occ_cell: int,
+    proposal: torch.Tensor,
+    skip_mode: int,
+    margin: float,
+) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor]:
+    if need_gvol and torch.are_deterministic_algorithms_enabled():
+        raise RuntimeError(
+            "Volume gradients on the cuda backend use nondeterministic atomics; "
+            "disable deterministic algorithms or detach the volume"
+        )
+    skip = _SkipArgs(occ_grid, occ_cell, proposal, skip_mode, margin, vol.shape)
+    return raymarch_backward(
+        go, vol, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam, skip=skip
+    )
+
+
+@fused_raymarch_skip_bwd.register_fake
+def _(go, vol, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam, *rest):
+    B, N, _ = tgt.shape
+    gM = torch.empty(B, 3, 4, device=M.device, dtype=torch.float32)
+    empty = gM.new_empty(0)
+    gvol = torch.empty(vol.shape, device=M.device, dtype=torch.float32) if need_gvol else empty
+    gsrc = torch.empty(src.shape, device=M.device, dtype=torch.float32) if need_gcam else empty
+    gtgt = torch.empty(B, N, 3, device=M.device, dtype=torch.float32) if need_gcam else empty
+    gstep = torch.empty(B, N, device=M.device, dtype=torch.float32) if need_gcam else empty
+    return gvol, gM, gsrc, gtgt, gstep
+
+
+def _skip_setup_context(ctx, inputs, output):
+    vol, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell, proposal, mode, margin = inputs
+    ctx.save_for_backward(vol, lab, M.contiguous(), src, tgt, step, occ_grid, proposal)
+    ctx.args = (n_samples, n_classes, width, occ_cell, mode, margin)
+
+
+def _skip_backward(ctx, go):
+    vol, lab, M, src, tgt, step, occ_grid, proposal = ctx.saved_tensors
+    n_samples, n_classes, width, occ_cell, mode, margin = ctx.args
+    need_gvol = ctx.needs_input_grad[0]
+    need_gcam = any(ctx.needs_input_grad[i] for i in (3, 4, 5))
+    gvol, gM, gsrc, gtgt, gstep = fused_raymarch_skip_bwd(
+        go, vol, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam,
+        occ_grid, occ_cell, proposal, mode, margin,
+    )
+    return (
+        gvol.to(vol.dtype) if need_gvol else None,
+        None,
+        gM.to(M.dtype),
+        gsrc.to(src.dtype) if need_gcam else None,
+        gtgt.to(tgt.dtype) if need_gcam else None,
+        gstep.to(step.dtype) if need_gcam else None,
+        None, None, None, None, None, None, None, None,
+    )
+
+
+torch.library.register_autograd(
+    "nanodrr_gb300::fused_raymarch_skip", _skip_backward, setup_context=_skip_setup_context
+)

@@ -27,7 +27,11 @@ class Registration(torch.nn.Module):
         self.register_buffer("sdd", sdd)
         self.height = height
         self.width = width
-        c = transform_point(rt_inv.inverse(), subject.isocenter[None].expand(rt_inv.shape[0], 3)[:, None])[:, 0]
+        # isocenter in camera coordinates; the 4x4 inverse is taken on the host
+        # in float64 (tiny, and it keeps CUDA linear-algebra libraries out of
+        # the render path)
+        inv = torch.linalg.inv(rt_inv.detach().double().cpu()).to(rt_inv)
+        c = transform_point(inv, subject.isocenter[None].expand(rt_inv.shape[0], 3)[:, None])[:, 0]
         self.register_buffer("pivot", self._make_translation(c))
         self.register_buffer("pivot_inv", self._make_translation(-c))
         nb = batch if batch is not None else 1

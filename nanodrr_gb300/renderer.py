@@ -15,7 +15,7 @@ from __future__ import annotations
 
 import torch
 
-from .raymarch import fused_raymarch
+from .raymarch import fused_raymarch, fused_raymarch_skip
 from .subject import Subject
 
 _BACKENDS = ("auto", "cuda", "triton")
@@ -37,7 +37,11 @@ def _make_tgt(k_inv, sdd, height, width, device, dtype) -> torch.Tensor:
         indexing="ij",
     )
     uv1 = torch.stack([u, v, torch.ones_like(u)], dim=-1).reshape(N, 3)
-    return sdd[:, None, None] * torch.einsum("bij,nj->bni", k_inv, uv1)
+    # K^-1 @ uv1 as three broadcast multiply-adds: no library GEMM for a 3x3
+    # product, so the call also runs under torch's deterministic mode.
+    k = k_inv[:, None]  # [B, 1, 3, 3]
+    rays = k[..., 0] * uv1[None, :, 0:1] + k[..., 1] * uv1[None, :, 1:2] + k[..., 2] * uv1[None, :, 2:3]
+    return sdd[:, None, None] * rays
 
 
 def _make_src(orthographic: bool, tgt: torch.Tensor, sdd: torch.Tensor) -> torch.Tensor:
@@ -48,6 +52,12 @@ def _make_src(orthographic: bool, tgt: torch.Tensor, sdd: torch.Tensor) -> torch
         return src
     B = tgt.shape[0]
     return torch.zeros(B, 1, 3, device=tgt.device, dtype=tgt.dtype)
+
+
+def _affine_product(A3: torch.Tensor, rt: torch.Tensor) -> torch.Tensor:
+    """(A @ rt)[:, :3, :] for A3 = A[:3] ([3, 4]) and rt [B, 4, 4], written as a
+    broadcast sum (camera -> voxel affine of the reference, backends.py:96)."""
+    return (A3[None, :, :, None] * rt[:, None, :, :]).sum(dim=2)
 
 
 def compact_label(subject: Subject) -> torch.Tensor:
@@ -74,13 +84,13 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
     C = subject.n_classes
     vol = subject.image[0, 0].contiguous()
     lab = compact_label(subject) if C > 1 else vol
-    M = (subject.world_to_voxel.float() @ rt_inv.float())[:, :3, :]
+    M = _affine_product(subject.world_to_voxel.float()[:3], rt_inv.float())
     B = max(M.shape[0], tgt.shape[0])
     if M.shape[0] != B:
         M = M.expand(B, -1, -1)
     if not fused_supported(subject, B, height * width):
         raise ValueError("inputs exceed the CUDA kernel's limits (int32 indexing)")
-    out = fused_raymarch(
+    args = (
         vol,
         lab,
         M.contiguous(),
@@ -91,6 +101,12 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
         C,
         width,
     )
+    skip = getattr(subject, "empty_space", None)
+    if skip is not None:
+        out = fused_raymarch_skip(*args, skip.grid.grid, skip.grid.cell, skip.packed, int(skip.mode),
+                                  float(skip.margin))
+    else:
+        out = fused_raymarch(*args)
     return out.reshape(B, C, height, width)
 
 
