@@ -199,6 +199,28 @@ NDRR_API int32_t ndrr_raymarch_bwd_workspace_bytes(const ndrr_raymarch_args* arg
  * accumulates the volume gradient with atomics (not bitwise deterministic). */
 NDRR_API int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* args, void* stream);
 
+/* Allocation-free adjoint: the same computation and arguments as
+ * ndrr_raymarch_bwd, but args->workspace is ignored and the per-tile pose
+ * partials go to a 4 MiB scratch array inside this library, so the call needs
+ * no device allocation at all. It is meant for callers that cannot allocate
+ * device memory where they run the adjoint: hosts that own every byte of
+ * device memory through their own pool and give plugins no allocator, and
+ * real-time loops in which a cudaMalloc (with its implicit synchronisation
+ * and unbounded latency) is not allowed. Limits and behaviour:
+ *   - at most 4 MiB of partials (16 floats per pose and detector tile, e.g.
+ *     65536 pose-tiles = 128 poses of 256 x 256 rays with 16 x 8 tiles);
+ *     larger calls fail with NDRR_ERR_LIMIT and a message;
+ *   - the array is held by every GPU that loads the library until exit;
+ *   - the first call on a device looks up the array's device address (a
+ *     set-up step); make that first call before any stream capture;
+ *   - all calls share the array, so calls that overlap on the GPU (for
+ *     example on two streams at once) race; each call writes every partial
+ *     it reads, so nothing needs clearing between calls;
+ *   - gvol is still accumulated into: the caller zeroes it.
+ * No counterpart in the reference, whose adjoint allocates its partials with
+ * the torch allocator on every call. */
+NDRR_API int32_t ndrr_raymarch_bwd_noalloc(const ndrr_raymarch_args* args, void* stream);
+
 /* ---- empty-space structures ---------------------------------------------- */
 typedef struct ndrr_occupancy_args {
     uint32_t struct_size;   /* sizeof(ndrr_occupancy_args) */

@@ -6,6 +6,7 @@
 // allocates device memory or synchronises.
 #include <cstdarg>
 #include <cstdio>
+#include <mutex>
 #include <string>
 
 #include "ndrr_launch.h"
@@ -207,3 +208,65 @@ int32_t ndrr_occupancy_build(const ndrr_occupancy_args* a, void* stream) {
 }
 
 }  // extern "C"
+
+// ===================================================== allocation-free adjoint
+// Some callers cannot allocate device memory where they run the adjoint:
+// hosts that own all device memory through their own pool and give plugins
+// no allocator (inference servers, engines with a fixed device budget), and
+// real-time loops where a cudaMalloc, with its implicit synchronisation and
+// unbounded latency, is not allowed. They still pass inputs and outputs; the
+// one scratch buffer the adjoint needs (the per-tile pose partials) lives in
+// the file-scope device array below, which every GPU that loads this library
+// holds until the process exits.
+namespace {
+
+// 4 MiB: 16 floats per (pose, detector tile); with the default 16 x 8 ray
+// tile that is room for 65536 (pose, tile) pairs, e.g. 128 poses of 256 x 256.
+constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device. The host-side
+// name of a __device__ array is only a stand-in, so the address is looked up
+// with cudaGetSymbolAddress, once per device, with that device current.
+cudaError_t noalloc_scratch(void** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (g_noalloc_ptr[dev] == nullptr) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[dev] = p;
+    }
+    *out = g_noalloc_ptr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+
+extern "C" int32_t ndrr_raymarch_bwd_noalloc(const ndrr_raymarch_args* a, void* stream) {
+    int32_t rc = validate_common(a);
+    if (rc != NDRR_OK) return rc;
+    if (a->B == 0 || a->N == 0) return ok();
+    const uint64_t need = ndrr::bwd_workspace_bytes(*a, ndrr::choose_shape(*a, 0));
+    if (need > kNoAllocScratchBytes)
+        return fail(NDRR_ERR_LIMIT,
+                    "the allocation-free adjoint holds %llu bytes of scratch but this call needs %llu "
+                    "(16 floats per pose and detector tile); use fewer poses per call, a larger tile, or "
+                    "ndrr_raymarch_bwd with a caller-provided workspace",
+                    (unsigned long long)kNoAllocScratchBytes, (unsigned long long)need);
+    void* scratch = nullptr;
+    const cudaError_t e = noalloc_scratch(&scratch);
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "scratch address lookup failed: %s", cudaGetErrorString(e));
+    ndrr_raymarch_args local = *a;
+    local.workspace = scratch;
+    local.workspace_bytes = kNoAllocScratchBytes;
+    return ndrr_raymarch_bwd(&local, stream);
+}
