@@ -58,6 +58,7 @@ def parse_args():
     p.add_argument("--method", default="learned", choices=["plain", "occupancy", "learned"])
     p.add_argument("--train-poses", type=int, default=16)
     p.add_argument("--prop-epochs", type=int, default=40)
+    p.add_argument("--no-batched", action="store_true", help="skip the uneven batched-launch measurement")
     return p.parse_args()
 
 
@@ -373,6 +374,11 @@ def run_ours(args, world, rank, local):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, sub, k_inv, sdd, rt)
+    uneven = None
+    if not args.no_batched:
+        del reg, skips
+        torch.cuda.empty_cache()
+        uneven = batched_uneven(args, dev)
     out = {
         "metric": "fwd+bwd DRR frames/s at 512^3/256^2, learned-skip vs plain kernel",
         "value": round(value, 2),
@@ -417,8 +423,94 @@ def run_ours(args, world, rank, local):
     }
     if cpu is not None:
         out["cpu_baseline"] = cpu
+    if uneven is not None:
+        out["batched_uneven"] = uneven
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def batched_uneven(args, dev, steps=5):
+    """64 requests over three phantom volumes (256^3 @ 1.5 mm, 512x512x300 @
+    0.8 mm, 384x384x600 @ 0.7 mm), detectors from {128, 200, 256, 384, 512}^2,
+    300-1000 samples/ray, poses as above; forward + pose adjoint. Compares a
+    loop of single render calls with the persistent batched launch replayed
+    from a CUDA graph (tile shapes from the autotuner)."""
+    import numpy as np
+
+    import nanodrr_gb300 as nd
+    from nanodrr_gb300 import phantom
+    from nanodrr_gb300.autotune import Autotuner
+    from nanodrr_gb300.batched import BatchedRenderer, RenderRequest
+
+    specs = [((256, 256, 256), (1.5, 1.5, 1.5)), ((300, 512, 512), (0.8, 0.8, 0.8)), ((600, 384, 384), (0.7, 0.7, 0.7))]
+    subs = [phantom.make_phantom(sh, sp, seed=10 + i, device=dev).subject(device=dev) for i, (sh, sp) in enumerate(specs)]
+    rng = np.random.default_rng(2024)
+    reqs = []
+    for i in range(64):
+        det = int(rng.choice([128, 200, 256, 384, 512]))
+        k_inv, sdd = phantom.detector(sdd=1020.0, pixel=1.2 * 256 / det, height=det, width=det)
+        reqs.append(RenderRequest(subs[int(rng.integers(0, 3))], k_inv.to(dev), sdd.to(dev), det, det,
+                                  int(rng.integers(300, 1001))))
+    poses = phantom.random_poses(64, seed=33).to(dev)
+    rays = sum(r.height * r.width for r in reqs)
+
+    # (a) a loop of single render calls: forward + pose backward
+    def loop():
+        for i, r in enumerate(reqs):
+            rt = poses[i : i + 1].clone().requires_grad_(True)
+            img = nd.render(r.subject, r.k_inv, rt, r.sdd, r.height, r.width, n_samples=r.n_samples)
+            img.sum().backward()
+
+    # (b) persistent batched kernel, whole step in a CUDA graph
+    tuner = Autotuner(None, reps=3)
+    t0 = time.perf_counter()
+    br = BatchedRenderer(reqs, autotuner=tuner)
+    tune_s = time.perf_counter() - t0
+    pose_in = poses.clone()
+
+    def step():
+        br.set_poses(pose_in)
+        br.forward()
+        br.go_flat.fill_(1.0)
+        br.backward()
+
+    step()
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    s.wait_stream(torch.cuda.current_stream())
+    with torch.cuda.stream(s):
+        step()
+    torch.cuda.current_stream().wait_stream(s)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        step()
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / steps
+
+    t_loop = timed(loop)
+    t_graph = timed(g.replay)
+    shapes = {}
+    for sh in br.shapes:
+        shapes[str(sh)] = shapes.get(str(sh), 0) + 1
+    return {
+        "workload": "64 requests, 3 volumes, detectors 128-512^2, 300-1000 samples, fwd + pose bwd",
+        "rays_per_step": rays,
+        "loop_of_render_calls_frames_per_s": round(64 / t_loop, 1),
+        "persistent_graph_frames_per_s": round(64 / t_graph, 1),
+        "speedup": round(t_loop / t_graph, 2),
+        "autotune_s": round(tune_s, 2),
+        "tile_shapes": shapes,
+    }
 
 
 def _peaks():

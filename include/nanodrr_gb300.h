@@ -221,6 +221,62 @@ NDRR_API int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* args, void* stream)
  * the torch allocator on every call. */
 NDRR_API int32_t ndrr_raymarch_bwd_noalloc(const ndrr_raymarch_args* args, void* stream);
 
+/* ---- persistent batched launch -------------------------------------------- *
+ * Many render requests — different volumes (same dtype), detector sizes and
+ * sample counts — marched by ONE persistent kernel: CTAs take (request, tile)
+ * work items from an atomic counter until all are done, so small requests do
+ * not leave the GPU idle and a whole batch is one launch (capturable in a CUDA
+ * graph: the descriptors and their device buffers stay fixed while the poses
+ * they point to change). Forward and pose/camera adjoint (no volume gradient).
+ * No counterpart in the reference, which renders one volume and one detector
+ * size per call. */
+typedef struct ndrr_request {
+    const void* vol;            /* [D, H, W] in the batch's vol_dtype          */
+    const void* lab;            /* label map (batch lab_dtype) or NULL if C==1 */
+    int32_t D, H, W;
+    int32_t N;                  /* rays                                         */
+    int32_t width;              /* detector width (rays form an image)          */
+    int32_t n_samples;          /* >= 2                                         */
+    int32_t src_per_ray;        /* 0: src [1, 3], 1: src [N, 3]                 */
+    int32_t tile_w, tile_h, sample_split; /* tile_w * tile_h * sample_split == 256 */
+    const float* M;             /* [3, 4] camera -> voxel                       */
+    const float* src;
+    const float* tgt;           /* [N, 3]                                       */
+    const float* step;          /* [N]                                          */
+    void* out;                  /* forward output [C, N] in vol_dtype           */
+    const void* go;             /* adjoint input [C, N] in go_dtype             */
+    float* gM;                  /* adjoint output [3, 4]                        */
+    float* gsrc;                /* [1 | N, 3] when need_gcam                    */
+    float* gtgt;                /* [N, 3] when need_gcam                        */
+    float* gstep;               /* [N] when need_gcam                           */
+} ndrr_request;
+
+typedef struct ndrr_batch_args {
+    uint32_t struct_size;       /* sizeof(ndrr_batch_args)                      */
+    uint32_t abi_version;
+    const ndrr_request* requests;   /* DEVICE array [n_requests]               */
+    const int32_t* tile_offsets;    /* DEVICE [n_requests + 1]: exclusive prefix
+                                       sums of each request's tile count        */
+    int32_t n_requests;
+    int32_t total_tiles;
+    int32_t vol_dtype, lab_dtype, go_dtype;
+    int32_t n_classes;
+    int32_t need_gcam;
+    int32_t ctas;               /* persistent CTAs, 0 = library default        */
+    void* workspace;            /* ndrr_batched_workspace_bytes                 */
+    uint64_t workspace_bytes;
+    int32_t reserved[4];
+} ndrr_batch_args;
+
+/* Host-side check of a request array before it is uploaded; also returns the
+ * number of tiles of each request (tiles[n]) so the caller can build the
+ * prefix sums. */
+NDRR_API int32_t ndrr_batch_validate(const ndrr_request* host_requests, int32_t n_requests, int32_t n_classes,
+                                     int32_t* tiles);
+NDRR_API int32_t ndrr_batched_workspace_bytes(int32_t total_tiles, uint64_t* bytes);
+NDRR_API int32_t ndrr_batched_fwd(const ndrr_batch_args* args, void* stream);
+NDRR_API int32_t ndrr_batched_bwd(const ndrr_batch_args* args, void* stream);
+
 /* ---- empty-space structures ---------------------------------------------- */
 typedef struct ndrr_occupancy_args {
     uint32_t struct_size;   /* sizeof(ndrr_occupancy_args) */

@@ -134,6 +134,10 @@ SIGNATURES: dict[str, tuple] = {
     ),
     "ndrr_raymarch_bwd": (ctypes.c_int32, [ctypes.POINTER(RaymarchArgs), ctypes.c_void_p]),
     "ndrr_raymarch_bwd_noalloc": (ctypes.c_int32, [ctypes.POINTER(RaymarchArgs), ctypes.c_void_p]),
+    "ndrr_batch_validate": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p]),
+    "ndrr_batched_workspace_bytes": (ctypes.c_int32, [ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64)]),
+    "ndrr_batched_fwd": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p]),
+    "ndrr_batched_bwd": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p]),
     "ndrr_occupancy_dims": (ctypes.c_int32, [ctypes.c_int32] * 4 + [_i32p] * 3),
     "ndrr_occupancy_build": (ctypes.c_int32, [ctypes.POINTER(OccupancyArgs), ctypes.c_void_p]),
     "ndrr_proposal_last_error": (ctypes.c_char_p, []),

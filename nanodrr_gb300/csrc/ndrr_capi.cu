@@ -9,6 +9,7 @@
 #include <mutex>
 #include <string>
 
+#include "ndrr_device.cuh"
 #include "ndrr_launch.h"
 
 namespace {
@@ -178,6 +179,59 @@ int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* a, void* stream) {
     if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "adjoint launch failed: %s", cudaGetErrorString(e));
     return ok();
 }
+
+int32_t ndrr_batch_validate(const ndrr_request* q, int32_t n, int32_t n_classes, int32_t* tiles) {
+    if (q == nullptr || tiles == nullptr || n < 0) return fail(NDRR_ERR_INVALID_ARGUMENT, "bad request array");
+    if (n_classes < 1 || n_classes > 64) return fail(NDRR_ERR_INVALID_ARGUMENT, "batched n_classes must be 1..64");
+    for (int32_t i = 0; i < n; ++i) {
+        const ndrr_request& r = q[i];
+        if (r.vol == nullptr || r.M == nullptr || r.src == nullptr || r.tgt == nullptr || r.step == nullptr)
+            return fail(NDRR_ERR_INVALID_ARGUMENT, "request %d: NULL geometry pointer", i);
+        if (n_classes > 1 && r.lab == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "request %d: no label map", i);
+        if (r.D < 1 || r.H < 1 || r.W < 1 || (long long)r.D * r.H * r.W >= kInt32Max)
+            return fail(NDRR_ERR_INVALID_ARGUMENT, "request %d: bad volume dims", i);
+        if (r.N < 1 || r.n_samples < 2) return fail(NDRR_ERR_INVALID_ARGUMENT, "request %d: N >= 1, n_samples >= 2", i);
+        if ((long long)n_classes * r.N >= kInt32Max) return fail(NDRR_ERR_LIMIT, "request %d: C*N too large", i);
+        if (r.tile_w % 8 || r.tile_h % 4 || r.tile_w < 8 || r.tile_h < 4 ||
+            r.tile_w * r.tile_h * r.sample_split != 256 ||
+            (r.sample_split != 1 && r.sample_split != 2 && r.sample_split != 4))
+            return fail(NDRR_ERR_INVALID_ARGUMENT,
+                        "request %d: tile_w (mult. of 8) * tile_h (mult. of 4) * sample_split (1/2/4) must be 256", i);
+        const ndrr::TileMap tm = ndrr::make_tilemap(r.N, r.width, r.tile_w, r.tile_h);
+        tiles[i] = tm.tiles;
+    }
+    return ok();
+}
+
+int32_t ndrr_batched_workspace_bytes(int32_t total_tiles, uint64_t* bytes) {
+    if (bytes == nullptr || total_tiles < 0) return fail(NDRR_ERR_INVALID_ARGUMENT, "bad argument");
+    *bytes = 256 + (uint64_t)total_tiles * 16 * sizeof(float);
+    return ok();
+}
+
+static int32_t batched_common(const ndrr_batch_args* a, bool backward, void* stream) {
+    if (a == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "args is NULL");
+    if (a->struct_size != sizeof(ndrr_batch_args) || a->abi_version != NDRR_ABI_VERSION)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "ndrr_batch_args size/version mismatch");
+    if (a->n_requests == 0 || a->total_tiles == 0) return ok();
+    if (a->n_requests < 0 || a->total_tiles < 0 || a->requests == nullptr || a->tile_offsets == nullptr)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "requests / tile_offsets missing");
+    if (!is_float_dtype(a->vol_dtype)) return fail(NDRR_ERR_DTYPE, "volume dtype %d unsupported", a->vol_dtype);
+    if (a->n_classes < 1 || a->n_classes > 64) return fail(NDRR_ERR_INVALID_ARGUMENT, "n_classes must be 1..64");
+    if (a->n_classes > 1 && !is_any_dtype(a->lab_dtype)) return fail(NDRR_ERR_DTYPE, "label dtype unsupported");
+    if (backward && !is_float_dtype(a->go_dtype)) return fail(NDRR_ERR_DTYPE, "go dtype unsupported");
+    uint64_t need = 0;
+    ndrr_batched_workspace_bytes(a->total_tiles, &need);
+    if (a->workspace == nullptr || a->workspace_bytes < need)
+        return fail(NDRR_ERR_WORKSPACE, "batched launch needs %llu workspace bytes", (unsigned long long)need);
+    const cudaError_t e = ndrr::launch_batched(*a, backward, sm_count_current(), reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "batched launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
+int32_t ndrr_batched_fwd(const ndrr_batch_args* a, void* stream) { return batched_common(a, false, stream); }
+
+int32_t ndrr_batched_bwd(const ndrr_batch_args* a, void* stream) { return batched_common(a, true, stream); }
 
 int32_t ndrr_occupancy_dims(int32_t D, int32_t H, int32_t W, int32_t cell, int32_t* gz, int32_t* gy, int32_t* gx) {
     if (gz == nullptr || gy == nullptr || gx == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "NULL output");

@@ -25,6 +25,7 @@ size_t brick_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
 
 cudaError_t launch_fwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
 cudaError_t launch_bwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
+cudaError_t launch_batched(const ndrr_batch_args& a, bool backward, int sm_count, cudaStream_t st);
 cudaError_t launch_occupancy(const void* vol, int vol_dtype, int D, int H, int W, int cell, int max_dist,
                              uint8_t* dist, uint8_t* scratch, cudaStream_t st);
 

@@ -195,14 +195,12 @@ __device__ __forceinline__ void skip_stats_add(const MarchParams& p, unsigned lo
 // ===================================================================== forward
 // SKIP: 0 no skipping, 1 occupancy window, 2 learned proposal + check.
 template <typename VT, typename OT, bool MULTI, int SKIP>
-__device__ __forceinline__ void fwd_body(const MarchParams& p) {
+__device__ __forceinline__ void fwd_body(const MarchParams& p, const int tile, const int b) {
     extern __shared__ float smem[];
     const int R = p.tw * p.th;
     const int NT = R * p.K;
     const int tid = threadIdx.x;
     const int r = tid % R, k = tid / R;
-    const int tile = blockIdx.x % p.tm.tiles;
-    const int b = blockIdx.x / p.tm.tiles;
     const int n = tile_ray(p.tm, p.N, p.tw, p.th, tile, r);
 
     float m[12];
@@ -305,13 +303,13 @@ __device__ __forceinline__ void fwd_body(const MarchParams& p) {
 
 template <typename VT, typename OT, bool MULTI, int SKIP>
 __global__ void __launch_bounds__(512, 2) raymarch_fwd_kernel(const MarchParams p) {
-    fwd_body<VT, OT, MULTI, SKIP>(p);
+    fwd_body<VT, OT, MULTI, SKIP>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles);
 }
 
 // Proposal mode: the tensor-core inference prologue needs more registers.
 template <typename VT, typename OT, bool MULTI>
 __global__ void __launch_bounds__(256, 3) raymarch_fwd_prop_kernel(const MarchParams p) {
-    fwd_body<VT, OT, MULTI, 2>(p);
+    fwd_body<VT, OT, MULTI, 2>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles);
 }
 
 // ===================================================================== adjoint
@@ -455,10 +453,11 @@ __device__ __forceinline__ void adjoint_samples(const MarchParams& p, const floa
 }
 
 // CTA epilogue shared by the adjoint kernels: fixed-order reduction of the
-// pose partials into `partials[blockIdx.x]`, and the per-ray camera
+// pose partials into `partials[slot]`, and the per-ray camera
 // gradients (summing the K sample chunks of each ray in order).
 template <bool GCAM>
-__device__ __forceinline__ void adjoint_epilogue(const MarchParams& p, const ThreadRay& tr, const AdjAcc& A,
+__device__ __forceinline__ void adjoint_epilogue(const MarchParams& p, const size_t slot, const ThreadRay& tr,
+                                                 const AdjAcc& A,
                                                  float* smem, int R, int NT, int r, int k) {
     const int tid = threadIdx.x;
     const bool shared_src = GCAM && !p.src_per_ray;
@@ -484,7 +483,7 @@ __device__ __forceinline__ void adjoint_epilogue(const MarchParams& p, const Thr
     if (tid < nterms) {
         float sum = wred[tid];
         for (int w = 1; w < nwarps; ++w) sum += wred[w * kPartialStride + tid];
-        p.partials[(size_t)blockIdx.x * kPartialStride + tid] = sum;
+        p.partials[slot * kPartialStride + tid] = sum;
     }
     if (GCAM) {
         __syncthreads();
@@ -521,14 +520,12 @@ __device__ __forceinline__ void adjoint_epilogue(const MarchParams& p, const Thr
 // Adjoint with direct global atomics for the volume gradient.
 // SKIP (only with GVOL false, see apply_skip): 0, 1 occupancy, 2 proposal.
 template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP>
-__device__ __forceinline__ void bwd_body(const MarchParams& p) {
+__device__ __forceinline__ void bwd_body(const MarchParams& p, const int tile, const int b, const size_t slot) {
     extern __shared__ float smem[];
     const int R = p.tw * p.th;
     const int NT = R * p.K;
     const int tid = threadIdx.x;
     const int r = tid % R, k = tid / R;
-    const int tile = blockIdx.x % p.tm.tiles;
-    const int b = blockIdx.x / p.tm.tiles;
     const int n = tile_ray(p.tm, p.N, p.tw, p.th, tile, r);
 
     float m[12];
@@ -553,17 +550,17 @@ __device__ __forceinline__ void bwd_body(const MarchParams& p) {
     A.zero();
     const DirectScatter sc{p.gvol, p.D, p.H, p.W};
     adjoint_samples<VT, MULTI, GVOL, GCAM>(p, m, tr, b, tr.s0, tr.s1, go_ray, A, sc);
-    adjoint_epilogue<GCAM>(p, tr, A, smem, R, NT, r, k);
+    adjoint_epilogue<GCAM>(p, slot, tr, A, smem, R, NT, r, k);
 }
 
 template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP>
 __global__ void __launch_bounds__(512, 1) raymarch_bwd_kernel(const MarchParams p) {
-    bwd_body<VT, MULTI, GVOL, GCAM, SKIP>(p);
+    bwd_body<VT, MULTI, GVOL, GCAM, SKIP>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles, blockIdx.x);
 }
 
 template <typename VT, bool MULTI, bool GCAM>
 __global__ void __launch_bounds__(256, 3) raymarch_bwd_prop_kernel(const MarchParams p) {
-    bwd_body<VT, MULTI, false, GCAM, 2>(p);
+    bwd_body<VT, MULTI, false, GCAM, 2>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles, blockIdx.x);
 }
 
 // Block-wide min of (a0..a2, -b0..-b2): the union box of per-thread boxes.
@@ -700,7 +697,7 @@ __global__ void __launch_bounds__(256, 2) raymarch_bwd_brick_kernel(const MarchP
         }
         sb = se;
     }
-    adjoint_epilogue<GCAM>(p, tr, A, smem, R, NT, tid, 0);
+    adjoint_epilogue<GCAM>(p, blockIdx.x, tr, A, smem, R, NT, tid, 0);
 }
 
 // Per-pose sum of the per-tile partials in a fixed order. One CTA per pose.

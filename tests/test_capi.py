@@ -132,3 +132,24 @@ def test_status_codes_map_to_reference_exceptions(lib):
         _ffi.check(lib.ndrr_raymarch_fwd(ctypes.byref(a), None), "fwd")
     with pytest.raises(RuntimeError):
         _ffi.check(_ffi.NDRR_ERR_CUDA, "fwd")
+
+
+def test_batch_validation_is_host_only_and_counts_tiles(lib):
+    from nanodrr_gb300.batched import BatchArgs, Request
+
+    assert ctypes.sizeof(Request) == 136
+    assert ctypes.sizeof(BatchArgs) == 88
+    arr = (Request * 2)()
+    for q, (n, w) in zip(arr, ((256 * 256, 256), (200 * 200, 200))):
+        q.vol = q.M = q.src = q.tgt = q.step = 0x1000
+        q.D = q.H = q.W = 64
+        q.N, q.width, q.n_samples = n, w, 100
+        q.tile_w, q.tile_h, q.sample_split = 16, 16, 1
+    tiles = (ctypes.c_int32 * 2)()
+    assert lib.ndrr_batch_validate(arr, 2, 1, tiles) == _ffi.NDRR_OK
+    assert list(tiles) == [16 * 16, 13 * 13]
+    arr[1].sample_split = 2  # 16 x 16 x 2 != 256 threads
+    assert lib.ndrr_batch_validate(arr, 2, 1, tiles) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert "request 1" in lib.ndrr_last_error().decode()
+    nb = ctypes.c_uint64()
+    assert lib.ndrr_batched_workspace_bytes(100, ctypes.byref(nb)) == 0 and nb.value == 256 + 100 * 64
