@@ -59,6 +59,8 @@ def parse_args():
     p.add_argument("--train-poses", type=int, default=16)
     p.add_argument("--prop-epochs", type=int, default=40)
     p.add_argument("--no-batched", action="store_true", help="skip the uneven batched-launch measurement")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the per-label forward and the 1024^2 learned-proposal measurements")
     return p.parse_args()
 
 
@@ -200,9 +202,9 @@ def run_ours(args, world, rank, local):
     import nanodrr_gb300 as nd
     from nanodrr_gb300 import _build
     from nanodrr_gb300.empty_space import EmptySpace, train_proposal
-    from nanodrr_gb300.raymarch import raymarch_backward, raymarch_forward
+    from nanodrr_gb300.raymarch import raymarch_backward, raymarch_forward, skip_windows
     from nanodrr_gb300.registration import NormalizedCrossCorrelation2d, Registration
-    from nanodrr_gb300.renderer import _affine_product, _make_src, _make_tgt
+    from nanodrr_gb300.renderer import _affine_product, _make_src, _make_tgt, cached_quad
 
     _build.build()
     dev = torch.device("cuda", local)
@@ -326,23 +328,33 @@ def run_ours(args, world, rank, local):
         occ_stats = torch.zeros(4, dtype=torch.int64, device=dev)
         raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, skip=skips["occupancy"], stats=occ_stats)
         gvol = torch.zeros_like(vol)
+        quad = cached_quad(sub, vol)
         reps = max(3, args.steps)
-        times = {"fwd": [], "fwd_learned": [], "bwd": []}
+        times = {"fwd": [], "fwd_learned": [], "bwd": [], "fwd_plain_layout": [], "bwd_plain_layout": [],
+                 "learned_windows": []}
         for i in range(reps + 1):
-            e = [torch.cuda.Event(enable_timing=True) for _ in range(6)]
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(8)]
             e[0].record()
-            raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd)
+            raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, quad=quad)
             e[1].record()
-            raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, skip=skips["learned"])
+            raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, skip=skips["learned"], quad=quad)
             e[2].record()
+            raymarch_backward(go, vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, True, True, gvol=gvol, quad=quad)
             e[3].record()
-            raymarch_backward(go, vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, True, True, gvol=gvol)
+            raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd)
             e[4].record()
+            raymarch_backward(go, vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, True, True, gvol=gvol)
+            e[5].record()
+            skip_windows(vol, M, srcb, tgtb, stepsz, S, Hd, skips["learned"])
+            e[6].record()
             torch.cuda.synchronize()
             if i > 0:
                 times["fwd"].append(e[0].elapsed_time(e[1]))
                 times["fwd_learned"].append(e[1].elapsed_time(e[2]))
-                times["bwd"].append(e[3].elapsed_time(e[4]))
+                times["bwd"].append(e[2].elapsed_time(e[3]))
+                times["fwd_plain_layout"].append(e[3].elapsed_time(e[4]))
+                times["bwd_plain_layout"].append(e[4].elapsed_time(e[5]))
+                times["learned_windows"].append(e[5].elapsed_time(e[6]))
     e_bytes = vol.element_size()
     fwd_bytes = n_samp * 8 * e_bytes
     bwd_bytes = n_samp * (8 * e_bytes + 4 + 8 * 4 * 2)
@@ -355,7 +367,7 @@ def run_ours(args, world, rank, local):
     ost = occ_stats.tolist()
     roofline = {
         "bound": "hbm",
-        "kernel": "raymarch_bwd_brick_kernel (adjoint with volume gradient)",
+        "kernel": "raymarch_bwd_kernel (adjoint with volume gradient, quad layout)",
         "achieved": round(achieved, 1),
         "peak": peaks["hbm_gbs"],
         "peak_source": peaks["source"],
@@ -366,19 +378,27 @@ def run_ours(args, world, rank, local):
         "samples_per_launch": n_samp,
         "fwd_ms": round(fwd_s * 1e3, 3),
         "fwd_learned_ms": round(fwdl_s * 1e3, 3),
+        "learned_windows_ms": round(statistics.median(times["learned_windows"]), 3),
         "bwd_ms": round(bwd_s * 1e3, 3),
         "fwd_gsamples_per_s": round(n_samp / fwd_s / 1e9, 2),
         "bwd_gsamples_per_s": round(n_samp / bwd_s / 1e9, 2),
         "fwd_frac_of_hbm": round(fwd_bytes / fwd_s / 1e9 / peaks["hbm_gbs"], 4),
+        "plain_layout_fwd_ms": round(statistics.median(times["fwd_plain_layout"]), 3),
+        "plain_layout_bwd_ms": round(statistics.median(times["bwd_plain_layout"]), 3),
     }
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, sub, k_inv, sdd, rt)
-    uneven = None
+    uneven = labels = leval = None
     if not args.no_batched:
         del reg, skips
         torch.cuda.empty_cache()
         uneven = batched_uneven(args, dev)
+    if not args.no_extras:
+        torch.cuda.empty_cache()
+        labels = per_label_forward(dev)
+        torch.cuda.empty_cache()
+        leval = learned_eval(dev)
     out = {
         "metric": "fwd+bwd DRR frames/s at 512^3/256^2, learned-skip vs plain kernel",
         "value": round(value, 2),
@@ -418,13 +438,19 @@ def run_ours(args, world, rank, local):
         "samples_per_s": round(n_samp * args.steps * world / t_dev, 1),
         "roofline": roofline,
         "e2e": e2e,
-        "gpu_launches": 3 * args.steps,
+        # per step: [window kernel (learned)], forward march, adjoint march,
+        # quad-gradient fold, per-pose reduction of the pose partials
+        "gpu_launches": (5 if headline == "learned" else 4) * args.steps,
         "clocks": clk,
     }
     if cpu is not None:
         out["cpu_baseline"] = cpu
     if uneven is not None:
         out["batched_uneven"] = uneven
+    if labels is not None:
+        out["per_label_forward"] = labels
+    if leval is not None:
+        out["learned_eval_1024"] = leval
     if rank == 0:
         print(json.dumps(out), flush=True)
 
@@ -511,6 +537,143 @@ def batched_uneven(args, dev, steps=5):
         "autotune_s": round(tune_s, 2),
         "tile_shapes": shapes,
     }
+
+
+def _event_ms(fn, steps):
+    """Median CUDA-event time of `fn` on the current stream (ms), after 3 warm-up calls."""
+    for _ in range(3):
+        fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return statistics.median(ts)
+
+
+def _rays(sub, rt, k_inv, sdd, det, S):
+    from nanodrr_gb300.renderer import _affine_product, _make_src, _make_tgt
+
+    dev = rt.device
+    M = _affine_product(sub.world_to_voxel[:3], rt).contiguous()
+    tgt = _make_tgt(k_inv, sdd, det, det, dev, torch.float32).expand(rt.shape[0], -1, -1).contiguous()
+    src = _make_src(False, tgt, sdd).contiguous()
+    step = ((tgt - src).norm(dim=-1) / (S - 1)).contiguous()
+    return M, src, tgt, step
+
+
+def _rel_maxabs(a, b):
+    """max over images of max|a - b| / max|b| (images = leading dims but the last)."""
+    a, b = a.float().flatten(0, -2), b.float().flatten(0, -2)
+    num = (a - b).abs().amax(-1)
+    den = b.abs().amax(-1).clamp_min(1e-30)
+    return float((num / den).max())
+
+
+def per_label_forward(dev, steps=5):
+    """Per-label forward on the 512 x 512 x 400 phantom (0.8 x 0.8 x 1.0 mm),
+    8 label channels plus the total, 32 poses, 256^2 detector at 1.2 mm, 800
+    samples/ray; the volume as float32 and as bf16 (quad layout, uint8 labels)."""
+    from nanodrr_gb300 import phantom
+    from nanodrr_gb300.raymarch import quad_volume, raymarch_forward
+    from nanodrr_gb300.renderer import compact_label
+
+    B, det, S, C = 32, 256, 800, 8
+    ph = phantom.make_phantom((400, 512, 512), (0.8, 0.8, 1.0), seed=0, device=dev)
+    sub = ph.subject(device=dev, with_labels=True)
+    del ph
+    lab = compact_label(sub)
+    k_inv, sdd = phantom.detector(sdd=1020.0, pixel=1.2, height=det, width=det)
+    M, src, tgt, step = _rays(sub, phantom.random_poses(B, seed=1).to(dev), k_inv.to(dev), sdd.to(dev), det, S)
+    vols = {"f32": sub.image[0, 0].contiguous()}
+    vols["bf16"] = vols["f32"].to(torch.bfloat16)
+    res = {"workload": "512x512x400 phantom, 8 labels + total, 32 poses, 256^2, 800 samples, forward",
+           "l2": "inputs larger than L2"}
+    outs = {}
+    for name, v in vols.items():
+        q = quad_volume(v)
+        fn = lambda: raymarch_forward(v, lab, M, src, tgt, step, S, C, det, with_total=True, quad=q)  # noqa: E731
+        ms = _event_ms(fn, steps)
+        outs[name] = fn()
+        res[name] = {"ms": round(ms, 3), "frames_per_s": round(B / ms * 1e3, 1)}
+        del q
+    res["bf16_vs_f32_rel_maxabs"] = {
+        "channels": round(_rel_maxabs(outs["bf16"][0], outs["f32"][0]), 5),
+        "total": round(_rel_maxabs(outs["bf16"][1], outs["f32"][1]), 5),
+    }
+    return res
+
+
+def learned_eval(dev, steps=5, epochs=40):
+    """Learned proposal against plain and occupancy-only marching: network
+    trained on 16 poses x 256^2 rays (about 1e6) of the 512 x 512 x 400
+    phantom, evaluated on 8 other poses at a 1024^2 detector with 1000
+    samples/ray, forward + backward (pose only, and pose + volume)."""
+    from nanodrr_gb300 import phantom
+    from nanodrr_gb300.empty_space import EmptySpace, train_proposal
+    from nanodrr_gb300.raymarch import quad_volume, raymarch_backward, raymarch_forward
+
+    ph = phantom.make_phantom((400, 512, 512), (0.8, 0.8, 1.0), seed=0, device=dev)
+    sub = ph.subject(device=dev)
+    del ph
+    vol = sub.image[0, 0].contiguous()
+    q = quad_volume(vol)
+    S_tr, S = 800, 1000
+    k_tr, sdd = phantom.detector(sdd=1020.0, pixel=1.2, height=256, width=256)
+    Mt, srct, tgtt, stept = _rays(sub, phantom.random_poses(16, seed=500).to(dev), k_tr.to(dev), sdd.to(dev), 256,
+                                  S_tr)
+    t0 = time.perf_counter()
+    net, hist = train_proposal(vol, Mt, srct, tgtt, stept, S_tr, 256, epochs=epochs, batch=65536, lr=2e-3,
+                               alpha=20.0)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t0
+    del Mt, srct, tgtt, stept
+    B, det = 8, 1024
+    k_ev, sdd = phantom.detector(sdd=1020.0, pixel=1.2 * 256 / det, height=det, width=det)
+    M, src, tgt, step = _rays(sub, phantom.random_poses(B, seed=7).to(dev), k_ev.to(dev), sdd.to(dev), det, S)
+    go = torch.randn(B, 1, det * det, device=dev)
+    gvol = torch.zeros_like(vol)
+    skips = {"plain": None, "occupancy": EmptySpace.occupancy(vol, cell=4),
+             "learned": EmptySpace.proposal(vol, net, cell=4, margin=2.0)}
+    res = {"workload": "512x512x400 phantom, 8 poses, 1024^2 detector, 1000 samples, fwd + bwd",
+           "train_rays": 16 * 256 * 256, "train_s": round(train_s, 2)}
+    ref = None
+    for name, es in skips.items():
+        def pose_step(es=es):
+            raymarch_forward(vol, vol, M, src, tgt, step, S, 1, det, quad=q, skip=es)
+            return raymarch_backward(go, vol, vol, M, src, tgt, step, S, 1, det, False, False, quad=q, skip=es)
+
+        def full_step(es=es):
+            raymarch_forward(vol, vol, M, src, tgt, step, S, 1, det, quad=q, skip=es)
+            return raymarch_backward(go, vol, vol, M, src, tgt, step, S, 1, det, True, False, gvol=gvol, quad=q,
+                                     skip=es)
+
+        ms_pose = _event_ms(pose_step, steps)
+        ms_full = _event_ms(full_step, steps)
+        stats = torch.zeros(4, dtype=torch.int64, device=dev)
+        out, _ = raymarch_forward(vol, vol, M, src, tgt, step, S, 1, det, quad=q, skip=es, stats=stats)
+        gM = pose_step()[1]
+        entry = {"pose_only_frames_per_s": round(B / ms_pose * 1e3, 1),
+                 "with_volume_grad_frames_per_s": round(B / ms_full * 1e3, 1)}
+        if es is not None:
+            st = stats.tolist()
+            entry["fallback_fraction"] = round(st[1] / max(1, st[0]), 4)
+            entry["marched_over_box_samples"] = round(st[2] / max(1, st[3]), 4)
+        if ref is None:
+            ref = (out, gM)
+        else:
+            entry["rel_maxabs_vs_plain"] = {"image": _rel_maxabs(out, ref[0]),
+                                            "pose_grad": _rel_maxabs(gM.flatten(1), ref[1].flatten(1))}
+        res[name] = entry
+    res["learned_vs_plain_pose_only"] = round(res["learned"]["pose_only_frames_per_s"]
+                                              / res["plain"]["pose_only_frames_per_s"], 3)
+    res["learned_vs_occupancy_pose_only"] = round(res["learned"]["pose_only_frames_per_s"]
+                                                  / res["occupancy"]["pose_only_frames_per_s"], 3)
+    return res
 
 
 def _peaks():

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define NDRR_ABI_VERSION 1
+#define NDRR_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define NDRR_API __attribute__((visibility("default")))
@@ -128,15 +128,17 @@ typedef struct ndrr_raymarch_args {
 
     /* Empty-space skipping (optional; see ndrr_occupancy_build).
      * skip_mode NDRR_SKIP_OCCUPANCY: each ray marches only between the first
-     * and last occupied grid cell it crosses. NDRR_SKIP_PROPOSAL: the learned
-     * proposal network (proposal_params, packed by ndrr_proposal_pack)
-     * predicts the non-empty interval inside the render kernel; the
-     * occupancy grid then checks that nothing occupied lies outside it, and
-     * rays that fail the check march their full box-culled window. Skipped
-     * samples have eight zero corners, so the image and the pose and camera
-     * gradients are unchanged; the volume gradient, which is non-zero on
-     * empty voxels too, always uses the full window (the adjoint ignores the
-     * skip when need_gvol is set). */
+     * and last occupied grid cell it crosses (computed inside the render
+     * kernels, or ahead of them by ndrr_skip_windows). NDRR_SKIP_PROPOSAL:
+     * the learned proposal network (proposal_params, packed by
+     * ndrr_proposal_pack) predicts the non-empty interval; the occupancy grid
+     * then checks that nothing occupied lies outside it, and rays that fail
+     * the check march their full box-culled window. The proposal is computed
+     * by ndrr_skip_windows only; the march entry points reject skip_mode 2
+     * (pass the windows as sample_window). Skipped samples have eight zero
+     * corners, so the image and the pose and camera gradients are unchanged;
+     * the volume gradient, which is non-zero on empty voxels too, always uses
+     * the full window (the adjoint ignores the skip when need_gvol is set). */
     int32_t skip_mode;
     int32_t occ_cell;
     int32_t occ_gx, occ_gy, occ_gz;
@@ -150,6 +152,24 @@ typedef struct ndrr_raymarch_args {
     float* out_extent;              /* optional [B, N, 2] forward output: t of
                                        the first and last sample with a
                                        non-zero corner, (1, 0) when none */
+
+    /* Quad layout (optional, built by ndrr_quad_build from `vol`): when
+     * vol_quad is set the kernels read each sample's eight corners with two
+     * vector loads from it instead of eight gathers from vol (same values,
+     * same results). The adjoint with need_gvol then also needs gvol_quad, a
+     * float32 scratch of ndrr_quad_dims elements x 16 bytes, which it zeroes,
+     * scatters into with two 16-byte reductions per sample and folds into
+     * gvol. Forward output in the volume's dtype only. */
+    const void* vol_quad;
+    float* gvol_quad;
+
+    /* Optional per-ray sample windows [B, N, 2] int32 (first sample, one
+     * past the last), as written by ndrr_skip_windows, or NULL. Each ray
+     * marches only the samples of its window (intersected with its box-culled
+     * window). It is an empty-space window: valid for the forward and the
+     * pose/camera adjoint, rejected together with need_gvol (the volume
+     * gradient needs every sample) or with skip_mode (one skip at a time). */
+    const int32_t* sample_window;
 
     /* Launch tuning; 0 selects the library default for each. */
     int32_t tile_w;         /* detector tile width in rays (8 or 16)            */
@@ -221,6 +241,20 @@ NDRR_API int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* args, void* stream)
  * the torch allocator on every call. */
 NDRR_API int32_t ndrr_raymarch_bwd_noalloc(const ndrr_raymarch_args* args, void* stream);
 
+/* Empty-space sample windows ahead of the march. For the rays of `args`
+ * (geometry, n_samples, optional t_window) and its skip_mode — OCCUPANCY:
+ * the distance-field walk to the first and last occupied cell; PROPOSAL: the
+ * learned network's interval, checked against the occupancy grid, with the
+ * full box-culled window for rays that fail the check — writes each ray's
+ * window [first sample, one past the last] to `windows` ([B, N, 2] int32,
+ * device) and adds to args->skip_stats when set. A march given these windows
+ * (args.sample_window, skip_mode 0) computes the same image and pose/camera
+ * gradients as one that skips in-kernel; one call serves the forward and the
+ * adjoint of a step. The network runs on the tensor cores (mma.sync, bf16
+ * operands, fp32 accumulation) in a persistent kernel that stages its weights
+ * in shared memory once per CTA. No counterpart in the reference. */
+NDRR_API int32_t ndrr_skip_windows(const ndrr_raymarch_args* args, int32_t* windows, void* stream);
+
 /* ---- persistent batched launch -------------------------------------------- *
  * Many render requests — different volumes (same dtype), detector sizes and
  * sample counts — marched by ONE persistent kernel: CTAs take (request, tile)
@@ -276,6 +310,15 @@ NDRR_API int32_t ndrr_batch_validate(const ndrr_request* host_requests, int32_t 
 NDRR_API int32_t ndrr_batched_workspace_bytes(int32_t total_tiles, uint64_t* bytes);
 NDRR_API int32_t ndrr_batched_fwd(const ndrr_batch_args* args, void* stream);
 NDRR_API int32_t ndrr_batched_bwd(const ndrr_batch_args* args, void* stream);
+
+/* ---- quad volume layout --------------------------------------------------- *
+ * Element (qz, qy, qx) holds the corners (x0, y0), (x0+1, y0), (x0, y0+1),
+ * (x0+1, y0+1) of plane z = qz - 2 with x0 = qx - 2, y0 = qy - 2, zeros
+ * outside the volume; extent (D + 4) x (H + 3) x (W + 3); element size 16 B
+ * for f32 volumes, 8 B for f16/bf16. No counterpart in the reference. */
+NDRR_API int32_t ndrr_quad_dims(int32_t D, int32_t H, int32_t W, int32_t* qz, int32_t* qy, int32_t* qx);
+NDRR_API int32_t ndrr_quad_build(const void* vol, int32_t vol_dtype, int32_t D, int32_t H, int32_t W, void* quad,
+                                 void* stream);
 
 /* ---- empty-space structures ---------------------------------------------- */
 typedef struct ndrr_occupancy_args {

@@ -25,7 +25,7 @@ NDRR_ERR_DEVICE_TIMEOUT = 6
 # ndrr_dtype
 NDRR_F32, NDRR_F16, NDRR_BF16, NDRR_U8, NDRR_I8, NDRR_I16, NDRR_I32, NDRR_I64 = range(8)
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 # ndrr_gvol_mode
 NDRR_GVOL_AUTO, NDRR_GVOL_DIRECT, NDRR_GVOL_BRICK = 0, 1, 2
@@ -81,6 +81,9 @@ class RaymarchArgs(ctypes.Structure):
         ("proposal_margin", ctypes.c_float),
         ("skip_stats", ctypes.c_void_p),
         ("out_extent", ctypes.c_void_p),
+        ("vol_quad", ctypes.c_void_p),
+        ("gvol_quad", ctypes.c_void_p),
+        ("sample_window", ctypes.c_void_p),
         ("tile_w", ctypes.c_int32),
         ("tile_h", ctypes.c_int32),
         ("sample_split", ctypes.c_int32),
@@ -138,8 +141,11 @@ SIGNATURES: dict[str, tuple] = {
     "ndrr_batched_workspace_bytes": (ctypes.c_int32, [ctypes.c_int32, ctypes.POINTER(ctypes.c_uint64)]),
     "ndrr_batched_fwd": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p]),
     "ndrr_batched_bwd": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p]),
+    "ndrr_quad_dims": (ctypes.c_int32, [ctypes.c_int32] * 3 + [_i32p] * 3),
+    "ndrr_quad_build": (ctypes.c_int32, [ctypes.c_void_p] + [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 2),
     "ndrr_occupancy_dims": (ctypes.c_int32, [ctypes.c_int32] * 4 + [_i32p] * 3),
     "ndrr_occupancy_build": (ctypes.c_int32, [ctypes.POINTER(OccupancyArgs), ctypes.c_void_p]),
+    "ndrr_skip_windows": (ctypes.c_int32, [ctypes.POINTER(RaymarchArgs), ctypes.c_void_p, ctypes.c_void_p]),
     "ndrr_proposal_last_error": (ctypes.c_char_p, []),
     "ndrr_proposal_dataset": (
         ctypes.c_int32,

@@ -34,18 +34,16 @@ template <typename VT, bool MULTI, bool GCAM>
 static cudaError_t bwd_dispatch_skip(const MarchParams& p, int skip, unsigned grid, unsigned block, size_t smem,
                                      cudaStream_t st) {
     if (skip == NDRR_SKIP_OCCUPANCY)
-        return launch_kernel(raymarch_bwd_kernel<VT, MULTI, false, GCAM, 1>, grid, block, smem, st, p);
-    if (skip == NDRR_SKIP_PROPOSAL)
-        return launch_kernel(raymarch_bwd_prop_kernel<VT, MULTI, GCAM>, grid, block, smem, st, p);
-    return launch_kernel(raymarch_bwd_kernel<VT, MULTI, false, GCAM, 0>, grid, block, smem, st, p);
+        return launch_kernel(raymarch_bwd_kernel<VT, MULTI, false, GCAM, 1, false>, grid, block, smem, st, p);
+    return launch_kernel(raymarch_bwd_kernel<VT, MULTI, false, GCAM, 0, false>, grid, block, smem, st, p);
 }
 
 template <typename VT, bool MULTI>
 static cudaError_t bwd_dispatch_flags(const MarchParams& p, bool gvol, bool gcam, int skip, unsigned grid,
                                       unsigned block, size_t smem, cudaStream_t st) {
     // With a volume gradient every sample matters: skipping never applies.
-    if (gvol && gcam) return launch_kernel(raymarch_bwd_kernel<VT, MULTI, true, true, 0>, grid, block, smem, st, p);
-    if (gvol) return launch_kernel(raymarch_bwd_kernel<VT, MULTI, true, false, 0>, grid, block, smem, st, p);
+    if (gvol && gcam) return launch_kernel(raymarch_bwd_kernel<VT, MULTI, true, true, 0, false>, grid, block, smem, st, p);
+    if (gvol) return launch_kernel(raymarch_bwd_kernel<VT, MULTI, true, false, 0, false>, grid, block, smem, st, p);
     if (gcam) return bwd_dispatch_skip<VT, MULTI, true>(p, skip, grid, block, smem, st);
     return bwd_dispatch_skip<VT, MULTI, false>(p, skip, grid, block, smem, st);
 }
@@ -58,13 +56,22 @@ static cudaError_t bwd_dispatch(const MarchParams& p, bool multi, bool gvol, boo
 }
 
 cudaError_t launch_bwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st) {
-    const MarchParams p = make_params(a, ls);
-    const unsigned grid = (unsigned)((size_t)a.B * p.tm.tiles);
-    const unsigned block = (unsigned)(ls.tw * ls.th * ls.K);
+    MarchParams p = make_params(a, ls);
     const bool multi = a.n_classes > 1, gvol = a.need_gvol != 0, gcam = a.need_gcam != 0;
     const int skip = gvol ? NDRR_SKIP_NONE : a.skip_mode;
+    unsigned grid = (unsigned)((size_t)a.B * p.tm.tiles);
+    const unsigned block = (unsigned)(ls.tw * ls.th * ls.K);
     cudaError_t e;
-    if (gvol && ls.brick) {
+    if (a.vol_quad != nullptr) {
+        // quad-layout gathers; with a volume gradient the taps go to the
+        // quad-layout gradient, zeroed here and folded into gvol below
+        if (gvol) {
+            e = cudaMemsetAsync(a.gvol_quad, 0, (size_t)(a.D + 4) * (a.H + 3) * (a.W + 3) * 16, st);
+            if (e != cudaSuccess) return e;
+        }
+        e = launch_bwd_quad(p, a.vol_dtype, multi, gvol, gcam, skip, grid, block, bwd_smem_bytes(a, ls), st);
+        if (e == cudaSuccess && gvol) e = launch_quad_fold(a.gvol_quad, a.D, a.H, a.W, a.gvol, st);
+    } else if (gvol && ls.brick) {
         e = launch_brick(a, ls, p, grid, block, st);
     } else {
         const size_t smem = bwd_smem_bytes(a, ls);

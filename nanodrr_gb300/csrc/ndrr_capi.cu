@@ -5,12 +5,12 @@
 // and adds the pointer/dtype/shape checks a C caller needs. Nothing here
 // allocates device memory or synchronises.
 #include <cstdarg>
+#include <cstdint>
 #include <cstdio>
 #include <mutex>
 #include <string>
 
-#include "ndrr_device.cuh"
-#include "ndrr_launch.h"
+#include "ndrr_march.cuh"
 
 namespace {
 
@@ -95,6 +95,12 @@ int32_t validate_common(const ndrr_raymarch_args* a) {
             return fail(NDRR_ERR_INVALID_ARGUMENT, "proposal skipping needs packed proposal parameters");
         if (!(a->proposal_margin >= 0.f)) return fail(NDRR_ERR_INVALID_ARGUMENT, "proposal_margin must be >= 0");
     }
+    if (reinterpret_cast<uintptr_t>(a->sample_window) % 8 != 0)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "sample_window must be 8-byte aligned");
+    if (a->sample_window != nullptr && a->skip_mode != NDRR_SKIP_NONE)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "sample_window and skip_mode are exclusive (one skip at a time)");
+    if (a->vol_quad != nullptr && (long long)(a->D + 4) * (a->H + 3) * (a->W + 3) >= kInt32Max)
+        return fail(NDRR_ERR_LIMIT, "quad layout of a %dx%dx%d volume exceeds int32 indexing", a->D, a->H, a->W);
     if (a->gvol_mode < NDRR_GVOL_AUTO || a->gvol_mode > NDRR_GVOL_BRICK)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode must be 0, 1 or 2 (got %d)", a->gvol_mode);
     if (a->reserved[0] < 0 || a->reserved[0] > 56 * 1024)
@@ -113,6 +119,14 @@ int32_t validate_shape(const ndrr::LaunchShape& ls, size_t smem) {
     return NDRR_OK;
 }
 
+// The learned proposal runs in the window kernel only (ndrr_skip_windows).
+int32_t reject_proposal_march(const ndrr_raymarch_args* a) {
+    if (a->skip_mode == NDRR_SKIP_PROPOSAL)
+        return fail(NDRR_ERR_INVALID_ARGUMENT,
+                    "skip_mode 2 (proposal) is computed by ndrr_skip_windows: pass its windows as sample_window");
+    return NDRR_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -120,22 +134,23 @@ extern "C" {
 int32_t ndrr_abi_version(void) { return NDRR_ABI_VERSION; }
 
 const char* ndrr_build_info(void) {
-    return "nanodrr_gb300 abi " "1" " sm_103a nvcc " __DATE__;
+    return "nanodrr_gb300 abi " "2" " sm_103a nvcc " __DATE__;
 }
 
 const char* ndrr_last_error(void) { return g_last_error.c_str(); }
 
 int32_t ndrr_raymarch_fwd(const ndrr_raymarch_args* a, void* stream) {
     int32_t rc = validate_common(a);
+    if (rc == NDRR_OK) rc = reject_proposal_march(a);
     if (rc != NDRR_OK) return rc;
     if (a->B == 0 || a->N == 0) return ok();
     if (a->out == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "out is NULL");
     if (!is_float_dtype(a->out_dtype)) return fail(NDRR_ERR_DTYPE, "out dtype %d unsupported", a->out_dtype);
     if (a->skip_mode != NDRR_SKIP_NONE && a->out_dtype != a->vol_dtype)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "empty-space skipping writes the output in the volume's dtype");
+    if (a->vol_quad != nullptr && a->out_dtype != a->vol_dtype)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "the quad layout writes the output in the volume's dtype");
     const ndrr::LaunchShape ls = ndrr::choose_shape(*a, sm_count_current());
-    if (a->skip_mode == NDRR_SKIP_PROPOSAL && ls.tw * ls.th * ls.K > 256)
-        return fail(NDRR_ERR_INVALID_ARGUMENT, "proposal skipping supports at most 256 threads per tile");
     rc = validate_shape(ls, ndrr::fwd_smem_bytes(*a, ls));
     if (rc != NDRR_OK) return rc;
     const cudaError_t e = ndrr::launch_fwd(*a, ls, reinterpret_cast<cudaStream_t>(stream));
@@ -158,14 +173,20 @@ int32_t ndrr_raymarch_bwd_workspace_bytes(const ndrr_raymarch_args* a, uint64_t*
 
 int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* a, void* stream) {
     int32_t rc = validate_common(a);
+    if (rc == NDRR_OK && !a->need_gvol) rc = reject_proposal_march(a);
     if (rc != NDRR_OK) return rc;
     if (a->B == 0 || a->N == 0) return ok();
     if (a->go == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "go is NULL");
     if (!is_float_dtype(a->go_dtype)) return fail(NDRR_ERR_DTYPE, "go dtype %d unsupported", a->go_dtype);
     if (a->gM == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "gM is NULL");
     if (a->need_gvol && a->gvol == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "need_gvol set but gvol is NULL");
+    if (a->need_gvol && a->sample_window != nullptr)
+        return fail(NDRR_ERR_INVALID_ARGUMENT,
+                    "sample_window cannot be combined with need_gvol: the volume gradient needs every sample");
     if (a->need_gcam && (a->gsrc == nullptr || a->gtgt == nullptr || a->gstep == nullptr))
         return fail(NDRR_ERR_INVALID_ARGUMENT, "need_gcam set but gsrc/gtgt/gstep is NULL");
+    if (a->vol_quad != nullptr && a->need_gvol && a->gvol_quad == nullptr)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "quad-layout adjoint with need_gvol needs gvol_quad scratch");
     // Workspace size depends on the tile shape only: check it before any
     // device query so a bad call fails without touching the GPU.
     const uint64_t need = ndrr::bwd_workspace_bytes(*a, ndrr::choose_shape(*a, 0));
@@ -177,6 +198,42 @@ int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* a, void* stream) {
     if (rc != NDRR_OK) return rc;
     const cudaError_t e = ndrr::launch_bwd(*a, ls, reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "adjoint launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
+int32_t ndrr_skip_windows(const ndrr_raymarch_args* a, int32_t* windows, void* stream) {
+    int32_t rc = validate_common(a);
+    if (rc != NDRR_OK) return rc;
+    if (a->skip_mode != NDRR_SKIP_OCCUPANCY && a->skip_mode != NDRR_SKIP_PROPOSAL)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "skip windows need skip_mode 1 (occupancy) or 2 (proposal)");
+    if (a->B == 0 || a->N == 0) return ok();
+    if (windows == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "windows is NULL");
+    if (reinterpret_cast<uintptr_t>(windows) % 8 != 0)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "windows must be 8-byte aligned");
+    const cudaError_t e = ndrr::launch_skip_windows(*a, windows, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "skip-window launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
+int32_t ndrr_quad_dims(int32_t D, int32_t H, int32_t W, int32_t* qz, int32_t* qy, int32_t* qx) {
+    if (qz == nullptr || qy == nullptr || qx == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "NULL output");
+    if (D < 1 || H < 1 || W < 1) return fail(NDRR_ERR_INVALID_ARGUMENT, "dims must be positive");
+    if ((long long)(D + 4) * (H + 3) * (W + 3) >= kInt32Max)
+        return fail(NDRR_ERR_LIMIT, "quad layout exceeds int32 indexing");
+    *qz = D + 4;
+    *qy = H + 3;
+    *qx = W + 3;
+    return ok();
+}
+
+int32_t ndrr_quad_build(const void* vol, int32_t dtype, int32_t D, int32_t H, int32_t W, void* quad, void* stream) {
+    if (vol == nullptr || quad == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "vol and quad must be non-NULL");
+    if (!is_float_dtype(dtype)) return fail(NDRR_ERR_DTYPE, "volume dtype %d unsupported", dtype);
+    int32_t qz, qy, qx;
+    int32_t rc = ndrr_quad_dims(D, H, W, &qz, &qy, &qx);
+    if (rc != NDRR_OK) return rc;
+    const cudaError_t e = ndrr::launch_quad_build(vol, dtype, D, H, W, quad, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "quad build failed: %s", cudaGetErrorString(e));
     return ok();
 }
 

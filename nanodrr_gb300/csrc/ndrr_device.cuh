@@ -14,6 +14,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 #include "../../include/nanodrr_gb300.h"
 
 namespace ndrr {
@@ -193,6 +195,106 @@ __device__ __forceinline__ void load_cell(const VT* __restrict__ vol, int D, int
     }
 }
 
+// ------------------------------------------------------------ quad layout
+// A padded copy of the volume in which element (qz, qy, qx) holds the four
+// corners (x0, y0), (x0 + 1, y0), (x0, y0 + 1), (x0 + 1, y0 + 1) of plane
+// z = qz - 2, with x0 = qx - 2 and y0 = qy - 2, zeros outside the volume.
+// Extent: QX = W + 3, QY = H + 3, QZ = D + 4 (cells with x0 in [-2, W],
+// y0 in [-2, H], both planes of z0 in [-2, D]). A sample then needs two
+// vector loads (planes z0 and z0 + 1) and no bounds checks: any position is
+// clamped into the zero border, where all corners are 0.
+template <typename VT>
+struct QuadOf;
+template <>
+struct QuadOf<float> {
+    using T = float4;
+};
+template <>
+struct QuadOf<__half> {
+    using T = uint2;
+};
+template <>
+struct QuadOf<__nv_bfloat16> {
+    using T = uint2;
+};
+
+struct QuadGeom {
+    int qx, qy;      // padded row length and rows per plane
+    int plane;       // qx * qy
+};
+
+__host__ __device__ __forceinline__ QuadGeom make_quadgeom(int D, int H, int W) {
+    (void)D;
+    QuadGeom g;
+    g.qx = W + 3;
+    g.qy = H + 3;
+    g.plane = g.qx * g.qy;
+    return g;
+}
+
+__device__ __forceinline__ void unpack_quad(float4 q, float& a, float& b, float& c, float& d) {
+    a = q.x;
+    b = q.y;
+    c = q.z;
+    d = q.w;
+}
+
+// bf16 -> f32 is exact: a bf16 value is the high half of the f32 bit pattern.
+__device__ __forceinline__ void unpack_quad_bf16(uint2 q, float& a, float& b, float& c, float& d) {
+    a = __uint_as_float(q.x << 16);
+    b = __uint_as_float(q.x & 0xffff0000u);
+    c = __uint_as_float(q.y << 16);
+    d = __uint_as_float(q.y & 0xffff0000u);
+}
+
+__device__ __forceinline__ void unpack_quad_f16(uint2 q, float& a, float& b, float& c, float& d) {
+    const __half2 h0 = *reinterpret_cast<const __half2*>(&q.x);
+    const __half2 h1 = *reinterpret_cast<const __half2*>(&q.y);
+    const float2 f0 = __half22float2(h0), f1 = __half22float2(h1);
+    a = f0.x;
+    b = f0.y;
+    c = f1.x;
+    d = f1.y;
+}
+
+// Quad index of the cell whose lower corner is the floor of (x, y, z),
+// clamped into the padded extent, plus the fractional offsets and the cell's
+// (clamped) corner indices for the gradient scatter.
+__device__ __forceinline__ int quad_cell(const QuadGeom& g, int D, int H, int W, float x, float y, float z,
+                                         Cell& c) {
+    x = fminf(fmaxf(x, -2.0f), (float)W + 1.0f);
+    y = fminf(fmaxf(y, -2.0f), (float)H + 1.0f);
+    z = fminf(fmaxf(z, -2.0f), (float)D + 1.0f);
+    const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+    c.fx = x - xf;
+    c.fy = y - yf;
+    c.fz = z - zf;
+    c.ix = min((int)xf, W);
+    c.iy = min((int)yf, H);
+    c.iz = min((int)zf, D);
+    return ((c.iz + 2) * g.qy + (c.iy + 2)) * g.qx + (c.ix + 2);
+}
+
+template <typename VT>
+__device__ __forceinline__ void load_cell_quad(const void* __restrict__ quad, const QuadGeom& g, int D, int H,
+                                               int W, float x, float y, float z, Cell& c) {
+    const int qi = quad_cell(g, D, H, W, x, y, z, c);
+    using Q = typename QuadOf<VT>::T;
+    const Q* __restrict__ qp = reinterpret_cast<const Q*>(quad);
+    const Q q0 = __ldg(qp + qi);
+    const Q q1 = __ldg(qp + qi + g.plane);
+    if constexpr (std::is_same<VT, float>::value) {
+        unpack_quad(q0, c.v000, c.v001, c.v010, c.v011);
+        unpack_quad(q1, c.v100, c.v101, c.v110, c.v111);
+    } else if constexpr (std::is_same<VT, __nv_bfloat16>::value) {
+        unpack_quad_bf16(q0, c.v000, c.v001, c.v010, c.v011);
+        unpack_quad_bf16(q1, c.v100, c.v101, c.v110, c.v111);
+    } else {
+        unpack_quad_f16(q0, c.v000, c.v001, c.v010, c.v011);
+        unpack_quad_f16(q1, c.v100, c.v101, c.v110, c.v111);
+    }
+}
+
 __device__ __forceinline__ float cell_value(const Cell& c) {
     const float c00 = fmaf(c.fx, c.v001 - c.v000, c.v000);
     const float c01 = fmaf(c.fx, c.v011 - c.v010, c.v010);
@@ -205,14 +307,19 @@ __device__ __forceinline__ float cell_value(const Cell& c) {
 
 // Analytic derivative of the trilinear interpolant with respect to the
 // voxel-space position (the partial derivatives of the formula above).
+// Written with explicit fmaf so every kernel instantiation rounds the same
+// way (the compiler would otherwise be free to contract differently).
 __device__ __forceinline__ void cell_grad(const Cell& c, float& gx, float& gy, float& gz) {
     const float wx0 = 1.f - c.fx, wy0 = 1.f - c.fy, wz0 = 1.f - c.fz;
-    gx = ((c.v001 - c.v000) * wy0 + (c.v011 - c.v010) * c.fy) * wz0 +
-         ((c.v101 - c.v100) * wy0 + (c.v111 - c.v110) * c.fy) * c.fz;
-    gy = ((c.v010 - c.v000) * wx0 + (c.v011 - c.v001) * c.fx) * wz0 +
-         ((c.v110 - c.v100) * wx0 + (c.v111 - c.v101) * c.fx) * c.fz;
-    gz = ((c.v100 - c.v000) * wx0 + (c.v101 - c.v001) * c.fx) * wy0 +
-         ((c.v110 - c.v010) * wx0 + (c.v111 - c.v011) * c.fx) * c.fy;
+    const float x00 = fmaf(c.v011 - c.v010, c.fy, __fmul_rn(c.v001 - c.v000, wy0));
+    const float x11 = fmaf(c.v111 - c.v110, c.fy, __fmul_rn(c.v101 - c.v100, wy0));
+    gx = fmaf(x11, c.fz, __fmul_rn(x00, wz0));
+    const float y00 = fmaf(c.v011 - c.v001, c.fx, __fmul_rn(c.v010 - c.v000, wx0));
+    const float y11 = fmaf(c.v111 - c.v101, c.fx, __fmul_rn(c.v110 - c.v100, wx0));
+    gy = fmaf(y11, c.fz, __fmul_rn(y00, wz0));
+    const float z00 = fmaf(c.v101 - c.v001, c.fx, __fmul_rn(c.v100 - c.v000, wx0));
+    const float z11 = fmaf(c.v111 - c.v011, c.fx, __fmul_rn(c.v110 - c.v010, wx0));
+    gz = fmaf(z11, c.fy, __fmul_rn(z00, wy0));
 }
 
 // Nearest-voxel label at (x, y, z); ties round to even like grid_sample's

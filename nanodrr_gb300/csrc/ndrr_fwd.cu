@@ -12,13 +12,11 @@ static cudaError_t fwd_dispatch_skip(const MarchParams& p, int skip, unsigned gr
                                      cudaStream_t st) {
     if constexpr (std::is_same<VT, OT>::value) {
         if (skip == NDRR_SKIP_OCCUPANCY)
-            return launch_kernel(raymarch_fwd_kernel<VT, OT, MULTI, 1>, grid, block, smem, st, p);
-        if (skip == NDRR_SKIP_PROPOSAL)
-            return launch_kernel(raymarch_fwd_prop_kernel<VT, OT, MULTI>, grid, block, smem, st, p);
+            return launch_kernel(raymarch_fwd_kernel<VT, OT, MULTI, 1, false>, grid, block, smem, st, p);
     } else {
         if (skip != NDRR_SKIP_NONE) return cudaErrorNotSupported;
     }
-    return launch_kernel(raymarch_fwd_kernel<VT, OT, MULTI, 0>, grid, block, smem, st, p);
+    return launch_kernel(raymarch_fwd_kernel<VT, OT, MULTI, 0, false>, grid, block, smem, st, p);
 }
 
 template <typename VT, typename OT>
@@ -41,12 +39,15 @@ static cudaError_t fwd_dispatch_out(const MarchParams& p, int out_dtype, bool mu
 
 cudaError_t launch_fwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st) {
     MarchParams p = make_params(a, ls);
-    p.prop_off = (fwd_base_bytes(a, ls) + 15) & ~(size_t)15;
-    const unsigned grid = (unsigned)((size_t)a.B * p.tm.tiles);
+    unsigned grid = (unsigned)((size_t)a.B * p.tm.tiles);
     const unsigned block = (unsigned)(ls.tw * ls.th * ls.K);
     const size_t smem = fwd_smem_bytes(a, ls);
     const bool multi = a.n_classes > 1;
     const int skip = a.skip_mode;
+    if (a.vol_quad != nullptr) {
+        if (a.out_dtype != a.vol_dtype) return cudaErrorNotSupported;
+        return launch_fwd_quad(p, a.vol_dtype, multi, skip, grid, block, smem, st);
+    }
     switch (a.vol_dtype) {
         case NDRR_F32: return fwd_dispatch_out<float>(p, a.out_dtype, multi, skip, grid, block, smem, st);
         case NDRR_F16: return fwd_dispatch_out<__half>(p, a.out_dtype, multi, skip, grid, block, smem, st);

@@ -49,6 +49,7 @@ struct MarchParams {
     int B, N, S;
     float inv_s;
     const float* t_window;
+    const int* win;  // per-ray sample windows [B * N][2] or NULL
     // forward
     void* out;
     void* out_total;
@@ -67,7 +68,10 @@ struct MarchParams {
     float margin;                   // widening of a proposed interval (samples)
     unsigned long long* stats;      // [4] counters or NULL
     float* out_extent;              // [B, N, 2] or NULL
-    size_t prop_off;                // byte offset of the proposal smem region
+    // quad layout (gathers from `quad`, volume-gradient scatter into `gquad`)
+    const void* quad;
+    float* gquad;
+    QuadGeom qg;
     // launch shape
     TileMap tm;
     int tw, th, K;
@@ -113,6 +117,11 @@ __device__ __forceinline__ void init_thread_ray(const MarchParams& p, const floa
         tr.ray.dz = m[8] * ex + m[9] * ey + m[10] * ez;
         ray_window(tr.ray, p.D, p.H, p.W, p.S);
         if (p.t_window) apply_t_window(tr.ray, __ldg(p.t_window + bn * 2), __ldg(p.t_window + bn * 2 + 1), p.S);
+        if (p.win) {
+            const int2 w = __ldg(reinterpret_cast<const int2*>(p.win) + bn);
+            tr.ray.lo = max(tr.ray.lo, w.x);
+            tr.ray.hi = max(min(tr.ray.hi, w.y), tr.ray.lo);
+        }
         tr.stepv = __ldg(p.step + bn);
     }
     tr.s0 = tr.ray.lo;
@@ -192,9 +201,20 @@ __device__ __forceinline__ void skip_stats_add(const MarchParams& p, unsigned lo
     }
 }
 
+// The eight corners of the sample's cell from the plain volume (bounds
+// checked per corner) or from the quad layout (two vector loads).
+template <typename VT, bool QUAD>
+__device__ __forceinline__ void fetch_cell(const MarchParams& p, float x, float y, float z, Cell& c) {
+    if constexpr (QUAD) {
+        load_cell_quad<VT>(p.quad, p.qg, p.D, p.H, p.W, x, y, z, c);
+    } else {
+        load_cell(reinterpret_cast<const VT*>(p.vol), p.D, p.H, p.W, x, y, z, c);
+    }
+}
+
 // ===================================================================== forward
-// SKIP: 0 no skipping, 1 occupancy window, 2 learned proposal + check.
-template <typename VT, typename OT, bool MULTI, int SKIP>
+// SKIP: 0 no skipping (or precomputed sample windows), 1 occupancy window.
+template <typename VT, typename OT, bool MULTI, int SKIP, bool QUAD = false>
 __device__ __forceinline__ void fwd_body(const MarchParams& p, const int tile, const int b) {
     extern __shared__ float smem[];
     const int R = p.tw * p.th;
@@ -212,16 +232,11 @@ __device__ __forceinline__ void fwd_body(const MarchParams& p, const int tile, c
     if (SKIP != 0) {
         const int box_len = max(tr.ray.hi - tr.ray.lo, 0);
         const bool has = n >= 0 && box_len > 0;
-        float pn = 0.f, pf = 1.f;
-        if (SKIP == 2)
-            proposal_window_cta(p.proposal, reinterpret_cast<unsigned char*>(smem) + p.prop_off, tr.ray, p.D, p.H,
-                                p.W, has, r, k, R, pn, pf);
-        const bool fell = apply_skip(p, tr, pn, pf);
+        const bool fell = apply_skip(p, tr, 0.f, 1.f);
         if (p.stats) skip_stats_add(p, p.stats, k, has, fell, box_len, max(tr.ray.hi - tr.ray.lo, 0));
     }
     chunk_thread_ray(tr, k, p.K);
 
-    const VT* __restrict__ vol = reinterpret_cast<const VT*>(p.vol);
     float acc = 0.f;
     int first = INT_MAX, last = -1;  // non-empty extent of this thread's chunk
     float* cacc = smem + tid;  // MULTI: per-thread class accumulators, stride NT
@@ -234,7 +249,7 @@ __device__ __forceinline__ void fwd_body(const MarchParams& p, const int tile, c
         const float y = fmaf(t, tr.ray.dy, tr.ray.p0y);
         const float z = fmaf(t, tr.ray.dz, tr.ray.p0z);
         Cell cell;
-        load_cell(vol, p.D, p.H, p.W, x, y, z, cell);
+        fetch_cell<VT, QUAD>(p, x, y, z, cell);
         const float val = cell_value(cell);
         acc += val;
         if (p.out_extent) {
@@ -301,15 +316,9 @@ __device__ __forceinline__ void fwd_body(const MarchParams& p, const int tile, c
     }
 }
 
-template <typename VT, typename OT, bool MULTI, int SKIP>
+template <typename VT, typename OT, bool MULTI, int SKIP, bool QUAD>
 __global__ void __launch_bounds__(512, 2) raymarch_fwd_kernel(const MarchParams p) {
-    fwd_body<VT, OT, MULTI, SKIP>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles);
-}
-
-// Proposal mode: the tensor-core inference prologue needs more registers.
-template <typename VT, typename OT, bool MULTI>
-__global__ void __launch_bounds__(256, 3) raymarch_fwd_prop_kernel(const MarchParams p) {
-    fwd_body<VT, OT, MULTI, 2>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles);
+    fwd_body<VT, OT, MULTI, SKIP, QUAD>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles);
 }
 
 // ===================================================================== adjoint
@@ -390,65 +399,119 @@ struct BrickScatter {
     }
 };
 
+// Volume-gradient scatter into the quad-layout gradient: the eight corner
+// contributions of a sample are two 16-byte vector reductions (planes z0 and
+// z0 + 1) at the sample's quad cell; ndrr_quad.cu folds the quad gradient
+// back into the volume's layout afterwards. Indices come clamped into the
+// padded extent, so no bounds checks are needed.
+struct QuadScatter {
+    float* __restrict__ gq;
+    QuadGeom g;
+    __device__ __forceinline__ void operator()(int, int ix, int iy, int iz, float g00, float g01, float g10,
+                                               float g11, float wx0, float wx1) const {
+        const int qi = ((iz + 2) * g.qy + (iy + 2)) * g.qx + (ix + 2);
+        float* a = gq + (size_t)qi * 4;
+        float* b = a + (size_t)g.plane * 4;
+        // No "memory" clobber: nothing in the adjoint reads the gradient, so
+        // the volume loads of later samples may be scheduled above these.
+        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(a), "f"(g00 * wx0), "f"(g00 * wx1),
+                     "f"(g01 * wx0), "f"(g01 * wx1));
+        asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(b), "f"(g10 * wx0), "f"(g10 * wx1),
+                     "f"(g11 * wx0), "f"(g11 * wx1));
+    }
+};
+
+// Upstream gradient of one sample: the ray's own for one channel, else the
+// one of the sample's label channel, with out-of-range labels masked like
+// the forward drops them (_fused.py:233-237).
+template <bool MULTI>
+__device__ __forceinline__ float sample_go(const MarchParams& p, int b, const ThreadRay& tr, float go_ray, float x,
+                                           float y, float z) {
+    if (!MULTI) return go_ray;
+    const int cls = nearest_label(p.lab, p.lab_dtype, p.D, p.H, p.W, x, y, z);
+    return ((unsigned)cls < (unsigned)p.C) ? ld_any_f(p.go, p.go_dtype, ((size_t)b * p.C + cls) * p.N + tr.n) : 0.f;
+}
+
+// Adjoint terms of one sample whose cell is loaded.
+template <bool GVOL, bool GCAM, typename Scatter>
+__device__ __forceinline__ void adjoint_accumulate(const float (&m)[12], const ThreadRay& tr, float t, float gg,
+                                                   const Cell& cell, AdjAcc& A, const Scatter& scatter);
+
 // Adjoint of samples [s0, s1) of one ray (reference _fused.py:230-298).
-template <typename VT, bool MULTI, bool GVOL, bool GCAM, typename Scatter>
+// Samples go in pairs: both pairs' loads are issued before either's
+// reductions, so two gathers per thread are in flight. The accumulation
+// order is the sample order either way.
+template <typename VT, bool MULTI, bool GVOL, bool GCAM, typename Scatter, bool QUAD = false>
 __device__ __forceinline__ void adjoint_samples(const MarchParams& p, const float (&m)[12], const ThreadRay& tr,
                                                 int b, int s0, int s1, float go_ray, AdjAcc& A,
                                                 const Scatter& scatter) {
-    const VT* __restrict__ vol = reinterpret_cast<const VT*>(p.vol);
-    for (int s = s0; s < s1; ++s) {
+    if (!MULTI && go_ray == 0.f) return;  // every term is proportional to go
+    int s = s0;
+    for (; s + 1 < s1; s += 2) {
+        const float ta = (float)s * p.inv_s, tb = (float)(s + 1) * p.inv_s;
+        const float xa = fmaf(ta, tr.ray.dx, tr.ray.p0x), xb = fmaf(tb, tr.ray.dx, tr.ray.p0x);
+        const float ya = fmaf(ta, tr.ray.dy, tr.ray.p0y), yb = fmaf(tb, tr.ray.dy, tr.ray.p0y);
+        const float za = fmaf(ta, tr.ray.dz, tr.ray.p0z), zb = fmaf(tb, tr.ray.dz, tr.ray.p0z);
+        const float ga = sample_go<MULTI>(p, b, tr, go_ray, xa, ya, za);
+        const float gb = sample_go<MULTI>(p, b, tr, go_ray, xb, yb, zb);
+        Cell ca, cb;
+        fetch_cell<VT, QUAD>(p, xa, ya, za, ca);
+        fetch_cell<VT, QUAD>(p, xb, yb, zb, cb);
+        if (ga != 0.f) adjoint_accumulate<GVOL, GCAM>(m, tr, ta, ga, ca, A, scatter);
+        if (gb != 0.f) adjoint_accumulate<GVOL, GCAM>(m, tr, tb, gb, cb, A, scatter);
+    }
+    if (s < s1) {
         const float t = (float)s * p.inv_s;
         const float x = fmaf(t, tr.ray.dx, tr.ray.p0x);
         const float y = fmaf(t, tr.ray.dy, tr.ray.p0y);
         const float z = fmaf(t, tr.ray.dz, tr.ray.p0z);
-        float gg = go_ray;
-        if (MULTI) {
-            // Upstream gradient of this sample's channel; out-of-range labels
-            // are masked like the forward drops them (_fused.py:233-237).
-            const int cls = nearest_label(p.lab, p.lab_dtype, p.D, p.H, p.W, x, y, z);
-            gg = ((unsigned)cls < (unsigned)p.C) ? ld_any_f(p.go, p.go_dtype, ((size_t)b * p.C + cls) * p.N + tr.n)
-                                                 : 0.f;
+        const float gg = sample_go<MULTI>(p, b, tr, go_ray, x, y, z);
+        if (gg != 0.f) {
+            Cell cell;
+            fetch_cell<VT, QUAD>(p, x, y, z, cell);
+            adjoint_accumulate<GVOL, GCAM>(m, tr, t, gg, cell, A, scatter);
         }
-        // Every adjoint term of this sample is proportional to gg.
-        if (gg == 0.f) continue;
-        const float g = gg * tr.stepv;
-        Cell cell;
-        load_cell(vol, p.D, p.H, p.W, x, y, z, cell);
-        float dvx, dvy, dvz;
-        cell_grad(cell, dvx, dvy, dvz);
-        const float gx = g * dvx, gy = g * dvy, gz = g * dvz;
-        const float qx = fmaf(t, tr.ex, tr.sx), qy = fmaf(t, tr.ey, tr.sy), qz = fmaf(t, tr.ez, tr.sz);
-        A.a[0] = fmaf(gx, qx, A.a[0]);
-        A.a[1] = fmaf(gx, qy, A.a[1]);
-        A.a[2] = fmaf(gx, qz, A.a[2]);
-        A.a[3] += gx;
-        A.a[4] = fmaf(gy, qx, A.a[4]);
-        A.a[5] = fmaf(gy, qy, A.a[5]);
-        A.a[6] = fmaf(gy, qz, A.a[6]);
-        A.a[7] += gy;
-        A.a[8] = fmaf(gz, qx, A.a[8]);
-        A.a[9] = fmaf(gz, qy, A.a[9]);
-        A.a[10] = fmaf(gz, qz, A.a[10]);
-        A.a[11] += gz;
-        if (GCAM) {
-            // Chain to camera space: gq = M[:, :3]^T gpos.
-            const float gqx = m[0] * gx + m[4] * gy + m[8] * gz;
-            const float gqy = m[1] * gx + m[5] * gy + m[9] * gz;
-            const float gqz = m[2] * gx + m[6] * gy + m[10] * gz;
-            const float omt = 1.f - t;
-            A.gsx = fmaf(omt, gqx, A.gsx);
-            A.gsy = fmaf(omt, gqy, A.gsy);
-            A.gsz = fmaf(omt, gqz, A.gsz);
-            A.gtx = fmaf(t, gqx, A.gtx);
-            A.gty = fmaf(t, gqy, A.gty);
-            A.gtz = fmaf(t, gqz, A.gtz);
-            A.gst = fmaf(gg, cell_value(cell), A.gst);
-        }
-        if (GVOL) {
-            const float wy0 = 1.f - cell.fy, wz0 = 1.f - cell.fz;
-            scatter(0, cell.ix, cell.iy, cell.iz, g * wz0 * wy0, g * wz0 * cell.fy, g * cell.fz * wy0,
-                    g * cell.fz * cell.fy, 1.f - cell.fx, cell.fx);
-        }
+    }
+}
+
+template <bool GVOL, bool GCAM, typename Scatter>
+__device__ __forceinline__ void adjoint_accumulate(const float (&m)[12], const ThreadRay& tr, float t, float gg,
+                                                   const Cell& cell, AdjAcc& A, const Scatter& scatter) {
+    const float g = gg * tr.stepv;
+    float dvx, dvy, dvz;
+    cell_grad(cell, dvx, dvy, dvz);
+    const float gx = g * dvx, gy = g * dvy, gz = g * dvz;
+    const float qx = fmaf(t, tr.ex, tr.sx), qy = fmaf(t, tr.ey, tr.sy), qz = fmaf(t, tr.ez, tr.sz);
+    A.a[0] = fmaf(gx, qx, A.a[0]);
+    A.a[1] = fmaf(gx, qy, A.a[1]);
+    A.a[2] = fmaf(gx, qz, A.a[2]);
+    A.a[3] += gx;
+    A.a[4] = fmaf(gy, qx, A.a[4]);
+    A.a[5] = fmaf(gy, qy, A.a[5]);
+    A.a[6] = fmaf(gy, qz, A.a[6]);
+    A.a[7] += gy;
+    A.a[8] = fmaf(gz, qx, A.a[8]);
+    A.a[9] = fmaf(gz, qy, A.a[9]);
+    A.a[10] = fmaf(gz, qz, A.a[10]);
+    A.a[11] += gz;
+    if (GCAM) {
+        // Chain to camera space: gq = M[:, :3]^T gpos.
+        const float gqx = m[0] * gx + m[4] * gy + m[8] * gz;
+        const float gqy = m[1] * gx + m[5] * gy + m[9] * gz;
+        const float gqz = m[2] * gx + m[6] * gy + m[10] * gz;
+        const float omt = 1.f - t;
+        A.gsx = fmaf(omt, gqx, A.gsx);
+        A.gsy = fmaf(omt, gqy, A.gsy);
+        A.gsz = fmaf(omt, gqz, A.gsz);
+        A.gtx = fmaf(t, gqx, A.gtx);
+        A.gty = fmaf(t, gqy, A.gty);
+        A.gtz = fmaf(t, gqz, A.gtz);
+        A.gst = fmaf(gg, cell_value(cell), A.gst);
+    }
+    if (GVOL) {
+        const float wy0 = 1.f - cell.fy, wz0 = 1.f - cell.fz;
+        scatter(0, cell.ix, cell.iy, cell.iz, g * wz0 * wy0, g * wz0 * cell.fy, g * cell.fz * wy0,
+                g * cell.fz * cell.fy, 1.f - cell.fx, cell.fx);
     }
 }
 
@@ -518,8 +581,8 @@ __device__ __forceinline__ void adjoint_epilogue(const MarchParams& p, const siz
 }
 
 // Adjoint with direct global atomics for the volume gradient.
-// SKIP (only with GVOL false, see apply_skip): 0, 1 occupancy, 2 proposal.
-template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP>
+// SKIP (only with GVOL false, see apply_skip): 0 none, 1 occupancy.
+template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP, bool QUAD = false>
 __device__ __forceinline__ void bwd_body(const MarchParams& p, const int tile, const int b, const size_t slot) {
     extern __shared__ float smem[];
     const int R = p.tw * p.th;
@@ -535,12 +598,7 @@ __device__ __forceinline__ void bwd_body(const MarchParams& p, const int tile, c
     init_thread_ray(p, m, b, n, tr);
     if (!GVOL && SKIP != 0) {
         // Skipped samples have eight zero corners: no pose or camera terms.
-        const bool has = n >= 0 && tr.ray.hi > tr.ray.lo;
-        float pn = 0.f, pf = 1.f;
-        if (SKIP == 2)
-            proposal_window_cta(p.proposal, reinterpret_cast<unsigned char*>(smem) + p.prop_off, tr.ray, p.D, p.H,
-                                p.W, has, r, k, R, pn, pf);
-        apply_skip(p, tr, pn, pf);
+        apply_skip(p, tr, 0.f, 1.f);
     }
     chunk_thread_ray(tr, k, p.K);
     float go_ray = 0.f;
@@ -548,19 +606,19 @@ __device__ __forceinline__ void bwd_body(const MarchParams& p, const int tile, c
 
     AdjAcc A;
     A.zero();
-    const DirectScatter sc{p.gvol, p.D, p.H, p.W};
-    adjoint_samples<VT, MULTI, GVOL, GCAM>(p, m, tr, b, tr.s0, tr.s1, go_ray, A, sc);
+    if constexpr (QUAD) {
+        const QuadScatter sc{p.gquad, p.qg};
+        adjoint_samples<VT, MULTI, GVOL, GCAM, QuadScatter, true>(p, m, tr, b, tr.s0, tr.s1, go_ray, A, sc);
+    } else {
+        const DirectScatter sc{p.gvol, p.D, p.H, p.W};
+        adjoint_samples<VT, MULTI, GVOL, GCAM>(p, m, tr, b, tr.s0, tr.s1, go_ray, A, sc);
+    }
     adjoint_epilogue<GCAM>(p, slot, tr, A, smem, R, NT, r, k);
 }
 
-template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP>
+template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP, bool QUAD>
 __global__ void __launch_bounds__(512, 1) raymarch_bwd_kernel(const MarchParams p) {
-    bwd_body<VT, MULTI, GVOL, GCAM, SKIP>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles, blockIdx.x);
-}
-
-template <typename VT, bool MULTI, bool GCAM>
-__global__ void __launch_bounds__(256, 3) raymarch_bwd_prop_kernel(const MarchParams p) {
-    bwd_body<VT, MULTI, false, GCAM, 2>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles, blockIdx.x);
+    bwd_body<VT, MULTI, GVOL, GCAM, SKIP, QUAD>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles, blockIdx.x);
 }
 
 // Block-wide min of (a0..a2, -b0..-b2): the union box of per-thread boxes.
@@ -703,6 +761,13 @@ __global__ void __launch_bounds__(256, 2) raymarch_bwd_brick_kernel(const MarchP
 // Per-pose sum of the per-tile partials in a fixed order. One CTA per pose.
 cudaError_t launch_brick(const ndrr_raymarch_args& a, const LaunchShape& ls, const MarchParams& p, unsigned grid,
                          unsigned block, cudaStream_t st);
+// Quad-layout instantiations live in their own translation units.
+cudaError_t launch_fwd_quad(const MarchParams& p, int vol_dtype, bool multi, int skip, unsigned grid,
+                            unsigned block, size_t smem, cudaStream_t st);
+cudaError_t launch_bwd_quad(const MarchParams& p, int vol_dtype, bool multi, bool gvol, bool gcam, int skip,
+                            unsigned grid, unsigned block, size_t smem, cudaStream_t st);
+cudaError_t launch_quad_fold(const float* gquad, int D, int H, int W, float* gvol, cudaStream_t st);
+cudaError_t launch_quad_build(const void* vol, int dtype, int D, int H, int W, void* quad, cudaStream_t st);
 
 MarchParams make_params(const ndrr_raymarch_args& a, const LaunchShape& ls);
 size_t fwd_base_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);

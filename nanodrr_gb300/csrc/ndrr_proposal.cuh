@@ -8,10 +8,11 @@
 // (f_near, f_far) of the in-box segment [tau0, tau1] where the non-empty
 // interval starts and ends; t_near = tau0 + f_near (tau1 - tau0).
 //
-// Inference inside the render kernels runs on the tensor cores with warp-level
-// mma.sync (bf16 operands, fp32 accumulation): a warp evaluates its 32 rays as
-// two 16-row tiles, keeping layer outputs in registers (an m16n8 f32
-// accumulator pair is exactly the A operand of the next m16n8k16 step).
+// Inference runs in the window kernel (ndrr_windows.cu), together with the
+// occupancy check, on the tensor cores with warp-level mma.sync (bf16
+// operands, fp32 accumulation): a warp evaluates its 32 rays as two 16-row
+// tiles, keeping layer outputs in registers (an m16n8 f32 accumulator pair is
+// exactly the A operand of the next m16n8k16 step).
 #pragma once
 
 #include "ndrr_device.cuh"
@@ -160,14 +161,13 @@ __device__ __forceinline__ void proposal_hidden_layer(const unsigned char* sm_w,
     }
 }
 
-// Proposed [pn, pf] (in t) for every ray of the CTA. Called by all threads;
+// Proposed [pn, pf] (in t) for every ray of the CTA's current item. Called by
+// all threads after proposal_stage_weights (done once per persistent CTA);
 // rays are CTA-local indices r in [0, R) owned by the threads with k == 0
 // (warps never mix k). `sm` is the proposal shared-memory region.
-__device__ __forceinline__ void proposal_window_cta(const unsigned char* __restrict__ packed, unsigned char* sm,
-                                                    const Ray& ray, int D, int H, int W, bool has, int r, int k,
-                                                    int R, float& pn, float& pf) {
-    proposal_stage_weights(packed, sm);
-    __syncthreads();
+__device__ __forceinline__ void proposal_window_cta(unsigned char* sm, const Ray& ray, int D, int H, int W,
+                                                    bool has, int r, int k, int R, float& pn, float& pf) {
+    __syncthreads();  // the previous tile is done with the result slots
     float* res = reinterpret_cast<float*>(sm + kSmStage + (R / 32) * kSmStageWarp);  // [R][2]
     const int lane = threadIdx.x & 31;
     if (k == 0) {

@@ -1,0 +1,87 @@
+// Quad volume layout: build (one pass over the padded extent) and the fold of
+// the quad-layout volume gradient back into the volume's layout. The layout
+// is defined in ndrr_device.cuh (QuadOf, make_quadgeom).
+#include "ndrr_march.cuh"
+
+namespace ndrr {
+
+template <typename VT>
+__device__ __forceinline__ VT ld_raw(const VT* p, long long idx) {
+    return p[idx];
+}
+
+// 32-bit float volume -> float4 quads.
+__global__ void quad_build_f32_kernel(const float* __restrict__ v, int D, int H, int W, float4* __restrict__ q) {
+    const int QX = W + 3, QY = H + 3;
+    const long long n = (long long)(D + 4) * QY * QX;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int qx = (int)(i % QX), qy = (int)((i / QX) % QY), qz = (int)(i / ((long long)QX * QY));
+        const int x0 = qx - 2, y0 = qy - 2, z = qz - 2;
+        float c[4] = {0.f, 0.f, 0.f, 0.f};
+        if ((unsigned)z < (unsigned)D) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int x = x0 + (k & 1), y = y0 + (k >> 1);
+                if ((unsigned)x < (unsigned)W && (unsigned)y < (unsigned)H) c[k] = v[((size_t)z * H + y) * W + x];
+            }
+        }
+        q[i] = make_float4(c[0], c[1], c[2], c[3]);
+    }
+}
+
+// 16-bit volume -> four raw 16-bit values per quad (bit-exact copies).
+__global__ void quad_build_b16_kernel(const uint16_t* __restrict__ v, int D, int H, int W, uint2* __restrict__ q) {
+    const int QX = W + 3, QY = H + 3;
+    const long long n = (long long)(D + 4) * QY * QX;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int qx = (int)(i % QX), qy = (int)((i / QX) % QY), qz = (int)(i / ((long long)QX * QY));
+        const int x0 = qx - 2, y0 = qy - 2, z = qz - 2;
+        uint32_t c[4] = {0u, 0u, 0u, 0u};
+        if ((unsigned)z < (unsigned)D) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int x = x0 + (k & 1), y = y0 + (k >> 1);
+                if ((unsigned)x < (unsigned)W && (unsigned)y < (unsigned)H) c[k] = v[((size_t)z * H + y) * W + x];
+            }
+        }
+        q[i] = make_uint2(c[0] | (c[1] << 16), c[2] | (c[3] << 16));
+    }
+}
+
+// gvol[z][y][x] += the four quad entries in which voxel (x, y) of plane z is
+// a corner: (x, y) as (x0, y0), (x0 + 1, y0), (x0, y0 + 1), (x0 + 1, y0 + 1).
+__global__ void quad_fold_kernel(const float4* __restrict__ gq, int D, int H, int W, float* __restrict__ gvol) {
+    const int QX = W + 3, QY = H + 3;
+    const long long n = (long long)D * H * W;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % W), y = (int)((i / W) % H), z = (int)(i / ((long long)W * H));
+        const size_t row = ((size_t)(z + 2) * QY + (y + 2)) * QX;
+        const size_t rowm = row - QX;  // y0 = y - 1
+        const float a = __ldg(&gq[row + x + 2].x);
+        const float b = __ldg(&gq[row + x + 1].y);
+        const float c = __ldg(&gq[rowm + x + 2].z);
+        const float d = __ldg(&gq[rowm + x + 1].w);
+        gvol[i] += (a + b) + (c + d);
+    }
+}
+
+static int grid_for(long long n) { return (int)std::max(1LL, std::min((n + 255) / 256, 152LL * 32)); }
+
+cudaError_t launch_quad_build(const void* vol, int dtype, int D, int H, int W, void* quad, cudaStream_t st) {
+    const long long n = (long long)(D + 4) * (H + 3) * (W + 3);
+    if (dtype == NDRR_F32)
+        quad_build_f32_kernel<<<grid_for(n), 256, 0, st>>>((const float*)vol, D, H, W, (float4*)quad);
+    else if (dtype == NDRR_F16 || dtype == NDRR_BF16)
+        quad_build_b16_kernel<<<grid_for(n), 256, 0, st>>>((const uint16_t*)vol, D, H, W, (uint2*)quad);
+    else
+        return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_quad_fold(const float* gquad, int D, int H, int W, float* gvol, cudaStream_t st) {
+    const long long n = (long long)D * H * W;
+    quad_fold_kernel<<<grid_for(n), 256, 0, st>>>((const float4*)gquad, D, H, W, gvol);
+    return cudaGetLastError();
+}
+
+}  // namespace ndrr

@@ -24,6 +24,7 @@ MarchParams make_params(const ndrr_raymarch_args& a, const LaunchShape& ls) {
     p.S = a.n_samples;
     p.inv_s = 1.0f / (float)(a.n_samples - 1);
     p.t_window = a.t_window;
+    p.win = a.sample_window;
     p.out = a.out;
     p.out_total = a.out_total;
     p.go = a.go;
@@ -43,7 +44,9 @@ MarchParams make_params(const ndrr_raymarch_args& a, const LaunchShape& ls) {
     p.margin = a.proposal_margin;
     p.stats = a.skip_stats;
     p.out_extent = a.out_extent;
-    p.prop_off = 0;
+    p.quad = a.vol_quad;
+    p.gquad = a.gvol_quad;
+    p.qg = make_quadgeom(a.D, a.H, a.W);
     p.tw = ls.tw;
     p.th = ls.th;
     p.K = ls.K;
@@ -53,6 +56,7 @@ MarchParams make_params(const ndrr_raymarch_args& a, const LaunchShape& ls) {
 
 LaunchShape choose_shape(const ndrr_raymarch_args& a, int sm_count) {
     LaunchShape ls;
+    ls.sm = sm_count;
     ls.tw = a.tile_w > 0 ? a.tile_w : 16;
     ls.th = a.tile_h > 0 ? a.tile_h : 8;
     const TileMap tm = make_tilemap(a.N, a.width, ls.tw, ls.th);
@@ -72,10 +76,7 @@ LaunchShape choose_shape(const ndrr_raymarch_args& a, int sm_count) {
     // which stays available on request.
     ls.brick = a.gvol_mode == NDRR_GVOL_BRICK;
     if (ls.tw * ls.th > 256) ls.brick = false;  // brick kernel is built for <= 256 threads
-    if (a.skip_mode == NDRR_SKIP_PROPOSAL) {
-        // the proposal kernels are built for <= 256 threads
-        while (ls.K > 1 && ls.tw * ls.th * ls.K > 256) ls.K >>= 1;
-    }
+    if (a.vol_quad != nullptr) ls.brick = false;  // the quad layout has its own scatter
     if (ls.brick) {
         ls.K = 1;
         const int nt = ls.tw * ls.th;
@@ -97,29 +98,24 @@ uint64_t bwd_workspace_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls)
     return (uint64_t)a.B * tm.tiles * kPartialStride * sizeof(float);
 }
 
-// Forward: class accumulators and chunk partials, then the extent scratch,
-// then (proposal mode) the network's region, which must not overlap them.
+// Forward: class accumulators and chunk partials, then the extent scratch.
 size_t fwd_base_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls) {
     const size_t NT = (size_t)ls.tw * ls.th * ls.K;
     const size_t ext = a.out_extent ? 2 * NT : 0;
     return ((a.n_classes > 1 ? (size_t)a.n_classes + 1 : 1) * NT + ext) * sizeof(float);
 }
 
-size_t fwd_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls) {
-    const size_t base = (fwd_base_bytes(a, ls) + 15) & ~(size_t)15;
-    return a.skip_mode == NDRR_SKIP_PROPOSAL ? base + proposal_smem_bytes(ls.tw * ls.th) : fwd_base_bytes(a, ls);
-}
+size_t fwd_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls) { return fwd_base_bytes(a, ls); }
 
-// Adjoint: the epilogue scratch; the proposal region (only used before the
-// march, when the adjoint skips) may alias it.
-size_t bwd_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls) {
+// Adjoint: the epilogue scratch, then (proposal mode, persistent CTAs that
+// keep the staged network across tiles) the network's region.
+size_t bwd_epilogue_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls) {
     const size_t NT = (size_t)ls.tw * ls.th * ls.K;
     const size_t wred = (NT / 32) * kPartialStride;
     const size_t cam = a.need_gcam ? 7 * NT : 0;
-    size_t bytes = std::max(wred, cam) * sizeof(float);
-    if (a.skip_mode == NDRR_SKIP_PROPOSAL && !a.need_gvol)
-        bytes = std::max(bytes, proposal_smem_bytes(ls.tw * ls.th));
-    return bytes;
+    return (std::max(wred, cam) * sizeof(float) + 15) & ~(size_t)15;
 }
+
+size_t bwd_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls) { return bwd_epilogue_bytes(a, ls); }
 
 }  // namespace ndrr

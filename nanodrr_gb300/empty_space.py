@@ -231,6 +231,11 @@ class EmptySpace:
     mode: int = _ffi.NDRR_SKIP_OCCUPANCY
     network: ProposalNetwork | None = None
     margin: float = 2.0  # samples of widening around a proposed interval
+    # True: the occupancy skip runs inside the render kernels; False: per-ray
+    # windows are computed first by their own kernel (ndrr_skip_windows) and
+    # shared by the forward and the pose/camera adjoint of a step. Same
+    # samples either way. The learned proposal always takes the window route.
+    fused: bool = True
 
     @property
     def packed(self) -> torch.Tensor:
@@ -239,13 +244,15 @@ class EmptySpace:
         return self.network.packed
 
     @classmethod
-    def occupancy(cls, vol: torch.Tensor, cell: int = 4, max_dist: int = 16) -> "EmptySpace":
-        return cls(OccupancyGrid.build(vol, cell, max_dist), _ffi.NDRR_SKIP_OCCUPANCY)
+    def occupancy(cls, vol: torch.Tensor, cell: int = 4, max_dist: int = 16, fused: bool = True) -> "EmptySpace":
+        return cls(OccupancyGrid.build(vol, cell, max_dist), _ffi.NDRR_SKIP_OCCUPANCY, fused=fused)
 
     @classmethod
     def proposal(cls, vol: torch.Tensor, network: ProposalNetwork, cell: int = 4, max_dist: int = 16,
                  margin: float = 2.0) -> "EmptySpace":
-        return cls(OccupancyGrid.build(vol, cell, max_dist), _ffi.NDRR_SKIP_PROPOSAL, network, margin)
+        """Learned proposal checked by the occupancy grid, evaluated by the
+        window kernel ahead of the march (ndrr_skip_windows)."""
+        return cls(OccupancyGrid.build(vol, cell, max_dist), _ffi.NDRR_SKIP_PROPOSAL, network, margin, False)
 
 
 def extents(vol, M, src, tgt, step, n_samples, width) -> torch.Tensor:

@@ -22,6 +22,18 @@ import math
 import torch
 
 
+def mm_small(A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
+    """A @ B for small (3x3, 4x4) matrices as one broadcast multiply and sum:
+    an elementwise kernel instead of a library GEMM launch per product, and
+    deterministic under torch's deterministic mode."""
+    return (A[..., :, :, None] * B[..., None, :, :]).sum(dim=-2)
+
+
+def mv_small(A: torch.Tensor, v: torch.Tensor) -> torch.Tensor:
+    """A @ v for small matrices and vectors (broadcast multiply and sum)."""
+    return (A * v[..., None, :]).sum(dim=-1)
+
+
 def _homo(v: torch.Tensor) -> torch.Tensor:
     return torch.cat([v, torch.ones_like(v[..., :1])], dim=-1)
 
@@ -80,8 +92,8 @@ def euler_to_rotmat(convention: str, angles: torch.Tensor) -> torch.Tensor:
         raise ValueError(f"bad Euler convention {convention!r}")
     mats = [_axis_rotation(ax.lower(), angles[..., i]) for i, ax in enumerate(convention)]
     if convention.isupper():
-        return mats[0] @ mats[1] @ mats[2]
-    return mats[2] @ mats[1] @ mats[0]
+        return mm_small(mm_small(mats[0], mats[1]), mats[2])
+    return mm_small(mm_small(mats[2], mats[1]), mats[0])
 
 
 def hat(v: torch.Tensor) -> torch.Tensor:
@@ -103,7 +115,7 @@ def rotvec_to_rotmat(v: torch.Tensor) -> torch.Tensor:
     b = torch.where(small, 0.5 - th2 / 24.0, (1.0 - torch.cos(th)) / th2s)
     K = hat(v)
     eye = torch.eye(3, dtype=v.dtype, device=v.device).expand_as(K)
-    return eye + a[..., None, None] * K + b[..., None, None] * (K @ K)
+    return eye + a[..., None, None] * K + b[..., None, None] * mm_small(K, K)
 
 
 def se3_V(v: torch.Tensor, eps: float = 1e-4) -> torch.Tensor:
@@ -115,7 +127,7 @@ def se3_V(v: torch.Tensor, eps: float = 1e-4) -> torch.Tensor:
     eye = torch.eye(3, dtype=v.dtype, device=v.device).expand_as(K)
     a = ((1.0 - torch.cos(th)) / th2)[..., None, None]
     b = ((th - torch.sin(th)) / (th2 * th))[..., None, None]
-    return eye + a * K + b * (K @ K)
+    return eye + a * K + b * mm_small(K, K)
 
 
 def make_se3(R: torch.Tensor, t: torch.Tensor) -> torch.Tensor:
@@ -138,7 +150,7 @@ def convert(
     t = R @ translation (+ isocenter), as the reference's `convert`."""
     if parameterization == "se3_log":
         R = rotvec_to_rotmat(rotation)
-        t = torch.einsum("...ij,...j->...i", se3_V(rotation), translation)
+        t = mv_small(se3_V(rotation), translation)
         return make_se3(R, t)
     if parameterization == "euler":
         if convention is None:
@@ -149,7 +161,7 @@ def convert(
         R = rotvec_to_rotmat(rotation)
     else:
         raise ValueError(f"unsupported parameterization {parameterization!r}")
-    t = torch.einsum("...ij,...j->...i", R, translation)
+    t = mv_small(R, translation)
     if isocenter is not None:
         t = t + isocenter
     return make_se3(R, t)
@@ -178,4 +190,4 @@ def make_rt_inv(
     a camera position relative to the isocenter: pose @ reorientation."""
     iso = isocenter if isocenter is not None else torch.zeros(3, device=rotation.device, dtype=rotation.dtype)
     pose = convert(rotation, translation, "euler", convention="ZXY", isocenter=iso)
-    return pose @ orientation_matrix(orientation, rotation.device, rotation.dtype)
+    return mm_small(pose, orientation_matrix(orientation, rotation.device, rotation.dtype))

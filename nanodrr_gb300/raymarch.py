@@ -119,6 +119,51 @@ def _apply_skip(a: _ffi.RaymarchArgs, skip, vol: torch.Tensor) -> None:
         a.proposal_params = skip.packed.data_ptr()
 
 
+def skip_windows(
+    vol: torch.Tensor,
+    M: torch.Tensor,
+    src: torch.Tensor,
+    tgt: torch.Tensor,
+    step: torch.Tensor,
+    n_samples: int,
+    width: int,
+    skip,
+    stats: torch.Tensor | None = None,
+    t_window: torch.Tensor | None = None,
+) -> torch.Tensor:
+    """Per-ray sample windows [B, N, 2] int32 (first sample, one past the
+    last) of an `EmptySpace` skip, computed by their own kernel
+    (ndrr_skip_windows); pass them to the march as `windows`."""
+    _check_inputs(vol, vol, M, src, tgt, step, n_samples, 1)
+    vol, _, M, src, tgt, step = _prep(vol, vol, M, src, tgt, step)
+    B, N, _ = tgt.shape
+    win = torch.empty(B, N, 2, device=vol.device, dtype=torch.int32)
+    a = _base_args(vol, vol, M, src, tgt, step, n_samples, 1, width)
+    _apply_skip(a, skip, vol)
+    if t_window is not None:
+        t_window = t_window.float().contiguous()
+        a.t_window = _ptr(t_window)
+    if stats is not None:
+        if stats.dtype != torch.int64 or stats.numel() < 4 or not stats.is_contiguous():
+            raise ValueError("stats must be a contiguous int64 tensor with 4 entries")
+        a.skip_stats = stats.data_ptr()
+    lib = _ffi.load()
+    _ffi.check(lib.ndrr_skip_windows(ctypes.byref(a), _ptr(win), _stream_handle(vol.device)), "ndrr_skip_windows")
+    return win
+
+
+def _windows_route(skip) -> bool:
+    """True when a skip is applied through per-ray windows: the learned
+    proposal always, the occupancy skip when built with fused=False."""
+    return skip is not None and (int(skip.mode) == _ffi.NDRR_SKIP_PROPOSAL or not getattr(skip, "fused", True))
+
+
+def _check_windows(win: torch.Tensor, B: int, N: int) -> torch.Tensor:
+    if win.dtype != torch.int32 or tuple(win.shape) != (B, N, 2):
+        raise ValueError(f"windows must be an int32 [B, N, 2] = [{B}, {N}, 2] tensor")
+    return win.contiguous()
+
+
 def _prep(vol, lab, M, src, tgt, step):
     vol = vol.contiguous()
     lab = lab.contiguous()
@@ -127,6 +172,24 @@ def _prep(vol, lab, M, src, tgt, step):
     tgt = tgt.float().contiguous()
     step = step.float().contiguous()
     return vol, lab, M, src, tgt, step
+
+
+def quad_volume(vol: torch.Tensor) -> torch.Tensor:
+    """Quad-layout copy of a [D, H, W] volume (see ndrr_quad_build): element
+    (qz, qy, qx) holds the four x/y corners of a cell of plane qz - 2, with a
+    zero border, so a trilinear sample is two vector loads."""
+    if not vol.is_cuda or vol.dim() != 3 or vol.dtype not in _FLOAT_DTYPES:
+        raise ValueError("quad_volume needs a [D, H, W] float CUDA tensor")
+    vol = vol.contiguous()
+    D, H, W = vol.shape
+    es = 16 if vol.dtype == torch.float32 else 8
+    q = torch.empty((D + 4) * (H + 3) * (W + 3) * es, device=vol.device, dtype=torch.uint8)
+    lib = _ffi.load()
+    _ffi.check(
+        lib.ndrr_quad_build(vol.data_ptr(), ndrr_dtype(vol), D, H, W, q.data_ptr(), _stream_handle(vol.device)),
+        "ndrr_quad_build",
+    )
+    return q
 
 
 def raymarch_forward(
@@ -146,16 +209,28 @@ def raymarch_forward(
     skip=None,
     extent: torch.Tensor | None = None,
     stats: torch.Tensor | None = None,
+    quad: torch.Tensor | None = None,
+    windows: torch.Tensor | None = None,
 ) -> tuple[torch.Tensor, torch.Tensor | None]:
     """Launch the forward kernel; returns (out [B, C, N], total [B, N] or None).
 
     `tile` optionally fixes the launch shape (tile_w, tile_h, sample_split).
     `skip` is an `EmptySpace` (empty-space skipping), `extent` an optional
     float32 [B, N, 2] output receiving each ray's non-empty interval in t,
-    `stats` an optional int64 [4] counter tensor (see ndrr_raymarch_args)."""
+    `stats` an optional int64 [4] counter tensor (see ndrr_raymarch_args),
+    `quad` the volume's quad-layout copy (`quad_volume`), read instead of
+    `vol` when given. The learned proposal, and an occupancy skip built with
+    `fused=False`, are applied through per-ray windows (`skip_windows`);
+    `windows` passes windows computed earlier."""
     _check_inputs(vol, lab, M, src, tgt, step, n_samples, n_classes)
     vol, lab, M, src, tgt, step = _prep(vol, lab, M, src, tgt, step)
     B, N, _ = tgt.shape
+    if _windows_route(skip):
+        if windows is None:
+            windows = skip_windows(vol, M, src, tgt, step, n_samples, width, skip, stats=stats, t_window=t_window)
+        skip, stats = None, None
+    if windows is not None:
+        windows = _check_windows(windows, B, N)
     odt = out_dtype or vol.dtype
     out = torch.empty(B, n_classes, N, device=vol.device, dtype=odt)
     total = torch.empty(B, N, device=vol.device, dtype=odt) if with_total else None
@@ -171,6 +246,10 @@ def raymarch_forward(
     if tile is not None:
         a.tile_w, a.tile_h, a.sample_split = (int(v) for v in tile)
     _apply_skip(a, skip, vol)
+    if windows is not None:
+        a.sample_window = _ptr(windows)
+    if quad is not None and quad.numel():
+        a.vol_quad = quad.data_ptr()
     if extent is not None:
         if extent.shape != (B, N, 2) or extent.dtype != torch.float32 or not extent.is_contiguous():
             raise ValueError("extent must be a contiguous float32 [B, N, 2] tensor")
@@ -203,6 +282,8 @@ def raymarch_backward(
     brick_cap: int = 0,
     tile: tuple[int, int, int] | None = None,
     skip=None,
+    quad: torch.Tensor | None = None,
+    windows: torch.Tensor | None = None,
 ):
     """Launch the adjoint; returns (gvol, gM, gsrc, gtgt, gstep) in float32.
 
@@ -211,10 +292,19 @@ def raymarch_backward(
     is allocated. `gvol_mode` selects the volume-gradient scatter (0 auto,
     1 direct atomics, 2 per-slab shared-memory brick), `brick_cap` the brick
     capacity in voxels (0 = default) and `tile` an explicit
-    (tile_w, tile_h, sample_split) launch shape."""
+    (tile_w, tile_h, sample_split) launch shape. Skips and `windows` apply to
+    the pose/camera adjoint only: with `need_gvol` every sample is marched."""
     _check_inputs(vol, lab, M, src, tgt, step, n_samples, n_classes)
     vol, lab, M, src, tgt, step = _prep(vol, lab, M, src, tgt, step)
     B, N, _ = tgt.shape
+    if need_gvol:
+        skip, windows = None, None
+    elif _windows_route(skip):
+        if windows is None:
+            windows = skip_windows(vol, M, src, tgt, step, n_samples, width, skip, t_window=t_window)
+        skip = None
+    if windows is not None:
+        windows = _check_windows(windows, B, N)
     dev = vol.device
     go = go.contiguous()
     if go.shape != (B, n_classes, N):
@@ -251,6 +341,15 @@ def raymarch_backward(
     a.gvol_mode = int(gvol_mode)
     a.reserved[0] = int(brick_cap)
     _apply_skip(a, skip, vol)
+    if windows is not None:
+        a.sample_window = _ptr(windows)
+    gq = None
+    if quad is not None and quad.numel():
+        a.vol_quad = quad.data_ptr()
+        if need_gvol:
+            D, H, W = vol.shape
+            gq = torch.empty((D + 4) * (H + 3) * (W + 3) * 4, device=dev, dtype=torch.float32)
+            a.gvol_quad = gq.data_ptr()
     if tile is not None:
         a.tile_w, a.tile_h, a.sample_split = (int(v) for v in tile)
     lib = _ffi.load()
@@ -357,11 +456,12 @@ def _backward(ctx, go):
 torch.library.register_autograd("nanodrr_gb300::fused_raymarch", _backward, setup_context=_setup_context)
 
 
-# ------------------------------------------------ empty-space-skipping op
-# Same contract as fused_raymarch plus the skip structures: an occupancy grid
-# (uint8 [gz, gy, gx]), its cell size, the packed proposal parameters (uint8,
-# empty for the occupancy mode), the mode and the interval margin. Skipped
-# samples have eight zero corners, so the output and the pose/camera
+# ------------------------------------------------------- general op
+# Same contract as fused_raymarch plus the layout and skip structures the
+# render call uses: `quad` is the volume's quad-layout copy (or an empty
+# tensor for the plain layout), `occ_grid`/`occ_cell`/`proposal`/`skip_mode`/
+# `margin` the empty-space skipping (skip_mode 0 = none; see EmptySpace).
+# Skipped samples have eight zero corners, so the output and the pose/camera
 # gradients equal the plain march's; the volume gradient is computed over the
 # full box-culled window.
 class _SkipArgs:
@@ -374,9 +474,16 @@ class _SkipArgs:
         self.margin = margin
 
 
-@torch.library.custom_op("nanodrr_gb300::fused_raymarch_skip", mutates_args=())
-def fused_raymarch_skip(
+def _skip_of(vol, occ_grid, occ_cell, proposal, skip_mode, margin):
+    if skip_mode == 0:
+        return None
+    return _SkipArgs(occ_grid, occ_cell, proposal, skip_mode, margin, vol.shape)
+
+
+@torch.library.custom_op("nanodrr_gb300::fused_raymarch_ex", mutates_args=())
+def fused_raymarch_ex(
     vol: torch.Tensor,
+    quad: torch.Tensor,
     lab: torch.Tensor,
     M: torch.Tensor,
     src: torch.Tensor,
@@ -390,22 +497,38 @@ def fused_raymarch_skip(
     proposal: torch.Tensor,
     skip_mode: int,
     margin: float,
-) -> torch.Tensor:
-    skip = _SkipArgs(occ_grid, occ_cell, proposal, skip_mode, margin, vol.shape)
-    out, _ = raymarch_forward(vol, lab, M, src, tgt, step, n_samples, n_classes, width, skip=skip)
-    return out
+    windows_ahead: bool,
+) -> tuple[torch.Tensor, torch.Tensor]:
+    """Returns (out [B, C, N], windows): with `windows_ahead` and a skip, the
+    per-ray sample windows [B, N, 2] int32 the forward used, which the
+    pose/camera adjoint reuses; otherwise an empty int32 tensor."""
+    skip = _skip_of(vol, occ_grid, occ_cell, proposal, skip_mode, margin)
+    windows = None
+    if skip is not None and (windows_ahead or _windows_route(skip)):
+        windows = skip_windows(vol, M, src, tgt, step, n_samples, width, skip)
+        skip = None
+    out, _ = raymarch_forward(vol, lab, M, src, tgt, step, n_samples, n_classes, width, skip=skip, quad=quad,
+                              windows=windows)
+    if windows is None:
+        windows = torch.empty(0, device=vol.device, dtype=torch.int32)
+    return out, windows
 
 
-@fused_raymarch_skip.register_fake
-def _(vol, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell, proposal, skip_mode, margin):
+@fused_raymarch_ex.register_fake
+def _(vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell, proposal, skip_mode,
+      margin, windows_ahead):
     B, N, _ = tgt.shape
-    return torch.empty(B, n_classes, N, device=vol.device, dtype=vol.dtype)
+    out = torch.empty(B, n_classes, N, device=vol.device, dtype=vol.dtype)
+    ahead = skip_mode == _ffi.NDRR_SKIP_PROPOSAL or (skip_mode != 0 and windows_ahead)
+    shape = (B, N, 2) if ahead else (0,)
+    return out, torch.empty(shape, device=vol.device, dtype=torch.int32)
 
 
-@torch.library.custom_op("nanodrr_gb300::fused_raymarch_skip_bwd", mutates_args=())
-def fused_raymarch_skip_bwd(
+@torch.library.custom_op("nanodrr_gb300::fused_raymarch_ex_bwd", mutates_args=())
+def fused_raymarch_ex_bwd(
     go: torch.Tensor,
     vol: torch.Tensor,
+    quad: torch.Tensor,
     lab: torch.Tensor,
     M: torch.Tensor,
     src: torch.Tensor,
@@ -421,20 +544,25 @@ def fused_raymarch_skip_bwd(
     proposal: torch.Tensor,
     skip_mode: int,
     margin: float,
+    windows: torch.Tensor,
 ) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor]:
     if need_gvol and torch.are_deterministic_algorithms_enabled():
         raise RuntimeError(
             "Volume gradients on the cuda backend use nondeterministic atomics; "
             "disable deterministic algorithms or detach the volume"
         )
-    skip = _SkipArgs(occ_grid, occ_cell, proposal, skip_mode, margin, vol.shape)
+    if windows.numel():
+        skip, win = None, windows
+    else:
+        skip, win = _skip_of(vol, occ_grid, occ_cell, proposal, skip_mode, margin), None
     return raymarch_backward(
-        go, vol, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam, skip=skip
+        go, vol, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam, skip=skip, quad=quad,
+        windows=win,
     )
 
 
-@fused_raymarch_skip_bwd.register_fake
-def _(go, vol, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam, *rest):
+@fused_raymarch_ex_bwd.register_fake
+def _(go, vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam, *rest):
     B, N, _ = tgt.shape
     gM = torch.empty(B, 3, 4, device=M.device, dtype=torch.float32)
     empty = gM.new_empty(0)
@@ -445,32 +573,32 @@ def _(go, vol, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, n
     return gvol, gM, gsrc, gtgt, gstep
 
 
-def _skip_setup_context(ctx, inputs, output):
-    vol, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell, proposal, mode, margin = inputs
-    ctx.save_for_backward(vol, lab, M.contiguous(), src, tgt, step, occ_grid, proposal)
+def _ex_setup_context(ctx, inputs, output):
+    (vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell, proposal, mode,
+     margin, windows_ahead) = inputs
+    ctx.save_for_backward(vol, quad, lab, M.contiguous(), src, tgt, step, occ_grid, proposal, output[1])
     ctx.args = (n_samples, n_classes, width, occ_cell, mode, margin)
 
 
-def _skip_backward(ctx, go):
-    vol, lab, M, src, tgt, step, occ_grid, proposal = ctx.saved_tensors
+def _ex_backward(ctx, go, _gwin):
+    vol, quad, lab, M, src, tgt, step, occ_grid, proposal, windows = ctx.saved_tensors
     n_samples, n_classes, width, occ_cell, mode, margin = ctx.args
     need_gvol = ctx.needs_input_grad[0]
-    need_gcam = any(ctx.needs_input_grad[i] for i in (3, 4, 5))
-    gvol, gM, gsrc, gtgt, gstep = fused_raymarch_skip_bwd(
-        go, vol, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam,
-        occ_grid, occ_cell, proposal, mode, margin,
+    need_gcam = any(ctx.needs_input_grad[i] for i in (4, 5, 6))
+    gvol, gM, gsrc, gtgt, gstep = fused_raymarch_ex_bwd(
+        go, vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam,
+        occ_grid, occ_cell, proposal, mode, margin, windows,
     )
     return (
         gvol.to(vol.dtype) if need_gvol else None,
-        None,
+        None,  # quad: a derived copy of vol
+        None,  # lab
         gM.to(M.dtype),
         gsrc.to(src.dtype) if need_gcam else None,
         gtgt.to(tgt.dtype) if need_gcam else None,
         gstep.to(step.dtype) if need_gcam else None,
-        None, None, None, None, None, None, None, None,
+        None, None, None, None, None, None, None, None, None,
     )
 
 
-torch.library.register_autograd(
-    "nanodrr_gb300::fused_raymarch_skip", _skip_backward, setup_context=_skip_setup_context
-)
+torch.library.register_autograd("nanodrr_gb300::fused_raymarch_ex", _ex_backward, setup_context=_ex_setup_context)

@@ -14,7 +14,7 @@ from __future__ import annotations
 
 import torch
 
-from .geometry import convert, transform_point
+from .geometry import convert, mm_small, transform_point
 from .renderer import render
 
 
@@ -41,7 +41,7 @@ class Registration(torch.nn.Module):
     @property
     def pose(self) -> torch.Tensor:
         T = convert(self._rot, self._xyz, "so3_log")
-        return self.rt_inv @ self.pivot @ T @ self.pivot_inv
+        return mm_small(mm_small(mm_small(self.rt_inv, self.pivot), T), self.pivot_inv)
 
     def forward(self, n_samples: int = 500, backend: str = "auto") -> torch.Tensor:
         return render(self.subject, self.k_inv, self.pose, self.sdd, self.height, self.width, n_samples,

@@ -15,7 +15,7 @@ from __future__ import annotations
 
 import torch
 
-from .raymarch import fused_raymarch, fused_raymarch_skip
+from .raymarch import fused_raymarch, fused_raymarch_ex, quad_volume
 from .subject import Subject
 
 _BACKENDS = ("auto", "cuda", "triton")
@@ -102,12 +102,34 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
         width,
     )
     skip = getattr(subject, "empty_space", None)
-    if skip is not None:
-        out = fused_raymarch_skip(*args, skip.grid.grid, skip.grid.cell, skip.packed, int(skip.mode),
-                                  float(skip.margin))
-    else:
+    # The quad copy is cached by the volume's address and version, which a
+    # traced graph cannot read: under torch.compile the plain layout is used.
+    compiling = hasattr(torch, "compiler") and torch.compiler.is_compiling()
+    layout = "plain" if compiling else getattr(subject, "layout", "quad")
+    if skip is None and layout == "plain":
         out = fused_raymarch(*args)
+    else:
+        quad = cached_quad(subject, vol) if layout == "quad" else vol.new_empty(0, dtype=torch.uint8)
+        empty = vol.new_empty(0, dtype=torch.uint8)
+        if skip is not None:
+            sk = (skip.grid.grid, skip.grid.cell, skip.packed, int(skip.mode), float(skip.margin),
+                  not getattr(skip, "fused", True))
+        else:
+            sk = (empty, 0, empty, 0, 0.0, False)
+        out = fused_raymarch_ex(args[0], quad, *args[1:], *sk)[0]
     return out.reshape(B, C, height, width)
+
+
+def cached_quad(subject, vol: torch.Tensor) -> torch.Tensor:
+    """The volume's quad-layout copy, rebuilt whenever the volume tensor or
+    its contents (version counter) change."""
+    key = (vol.data_ptr(), vol._version, vol.dtype, tuple(vol.shape), vol.device)
+    cache = getattr(subject, "_ndrr_quad_cache", None)
+    if cache is not None and cache[0] == key:
+        return cache[1]
+    q = quad_volume(vol.detach())
+    object.__setattr__(subject, "_ndrr_quad_cache", (key, q))
+    return q
 
 
 def render(

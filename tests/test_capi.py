@@ -42,7 +42,7 @@ def test_abi_version_and_struct_layout(lib):
     assert lib.ndrr_abi_version() == _ffi.ABI_VERSION
     assert b"sm_103a" in lib.ndrr_build_info()
     # 64-bit layout of ndrr_raymarch_args as declared in the header
-    assert ctypes.sizeof(_ffi.RaymarchArgs) == 312
+    assert ctypes.sizeof(_ffi.RaymarchArgs) == 336
     assert ctypes.sizeof(_ffi.OccupancyArgs) == 56
 
 
@@ -153,3 +153,33 @@ def test_batch_validation_is_host_only_and_counts_tiles(lib):
     assert "request 1" in lib.ndrr_last_error().decode()
     nb = ctypes.c_uint64()
     assert lib.ndrr_batched_workspace_bytes(100, ctypes.byref(nb)) == 0 and nb.value == 256 + 100 * 64
+
+
+def test_sample_window_rules_are_host_only(lib):
+    a = _valid_args()
+    a.sample_window = 0x7004  # not 8-byte aligned
+    assert lib.ndrr_raymarch_fwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert "aligned" in lib.ndrr_last_error().decode()
+    a.sample_window = 0x7000
+    a.skip_mode = _ffi.NDRR_SKIP_OCCUPANCY
+    a.occ_grid, a.occ_cell = 0x8000, 4
+    a.occ_gx = a.occ_gy = a.occ_gz = 4
+    assert lib.ndrr_raymarch_fwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert "exclusive" in lib.ndrr_last_error().decode()
+    b = _valid_args()
+    b.sample_window = 0x7000
+    b.go, b.go_dtype, b.gM = 0x4000, _ffi.NDRR_F32, 0x5000
+    b.need_gvol, b.gvol = 1, 0x9000
+    assert lib.ndrr_raymarch_bwd(ctypes.byref(b), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert "every sample" in lib.ndrr_last_error().decode()
+
+
+def test_skip_windows_validation(lib):
+    a = _valid_args()
+    assert lib.ndrr_skip_windows(ctypes.byref(a), 0x7000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT  # no skip mode
+    a.skip_mode = _ffi.NDRR_SKIP_OCCUPANCY
+    a.occ_grid, a.occ_cell = 0x8000, 4
+    a.occ_gx = a.occ_gy = a.occ_gz = 4
+    assert lib.ndrr_skip_windows(ctypes.byref(a), None, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert "windows is NULL" in lib.ndrr_last_error().decode()
+    assert lib.ndrr_skip_windows(ctypes.byref(a), 0x7002, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT

@@ -137,3 +137,78 @@ def test_render_with_empty_space_through_autograd():
     (img2 * w).sum().backward()
     assert rel_maxabs(img2, img) < 1e-6
     assert rel_maxabs(rt2.grad, rt1.grad) < 1e-5
+
+
+def _trained(seed=7):
+    ph, sub, vol, lab, M, src, tgt, step, n, det, k_inv, sdd, rt = _case(B=16, det=32, seed=seed)
+    net, _ = train_proposal(vol, M, src, tgt, step, n, det, epochs=150, batch=4096, lr=3e-3)
+    return vol, net, n, det
+
+
+def test_trained_proposal_adjoint_equals_plain():
+    """Skipped samples have eight zero corners, so the pose and camera
+    gradients equal the plain march's. A sample with a tiny value near the
+    body surface still has a full-size position gradient, so this is a
+    stricter check than the image."""
+    vol, net, n, det = _trained()
+    *_, M2, src2, tgt2, step2, _, _, _, _, _ = _case(B=4, det=32, seed=99)
+    skip = EmptySpace.proposal(vol, net, cell=4, margin=2.0)
+    go = torch.randn(4, 1, det * det, device=DEV)
+    plain, _ = raymarch_forward(vol, vol, M2, src2, tgt2, step2, n, 1, det)
+    fast, _ = raymarch_forward(vol, vol, M2, src2, tgt2, step2, n, 1, det, skip=skip)
+    # same non-zero samples; a sample split groups them differently (fp32 sums)
+    assert rel_maxabs(fast, plain) < 1e-6
+    pg = raymarch_backward(go, vol, vol, M2, src2, tgt2, step2, n, 1, det, False, True)
+    sg = raymarch_backward(go, vol, vol, M2, src2, tgt2, step2, n, 1, det, False, True, skip=skip)
+    for name, a, b in zip(("gM", "gsrc", "gtgt", "gstep"), sg[1:], pg[1:]):
+        assert rel_maxabs(a, b) < 1e-5, name
+
+
+@pytest.mark.parametrize("mode", ["occupancy", "proposal"])
+def test_skip_windows_equal_in_kernel_skipping(mode):
+    """Windows from ndrr_skip_windows give the in-kernel occupancy skip's
+    samples (bitwise image, same counters) and the plain march's image (up
+    to the grouping of fp32 sums under a sample split); the volume adjoint
+    ignores them."""
+    from nanodrr_gb300.raymarch import skip_windows
+
+    vol, net, n, det = _trained()
+    *_, M2, src2, tgt2, step2, _, _, _, _, _ = _case(B=4, det=32, seed=98)
+    if mode == "occupancy":
+        ahead = EmptySpace.occupancy(vol, cell=4, fused=False)
+    else:
+        ahead = EmptySpace.proposal(vol, net, cell=4, margin=2.0)
+    plain, _ = raymarch_forward(vol, vol, M2, src2, tgt2, step2, n, 1, det)
+    s2 = torch.zeros(4, dtype=torch.int64, device=DEV)
+    win = skip_windows(vol, M2, src2, tgt2, step2, n, det, ahead, stats=s2)
+    b, _ = raymarch_forward(vol, vol, M2, src2, tgt2, step2, n, 1, det, windows=win)
+    assert rel_maxabs(b, plain) < 1e-6
+    assert win.dtype == torch.int32 and win.shape == (4, det * det, 2)
+    assert bool((win[..., 0] <= win[..., 1]).all())
+    rays, fallbacks, marched, boxed = s2.tolist()
+    assert rays > 0 and marched < boxed
+    if mode == "occupancy":
+        s1 = torch.zeros(4, dtype=torch.int64, device=DEV)
+        a, _ = raymarch_forward(vol, vol, M2, src2, tgt2, step2, n, 1, det, skip=EmptySpace.occupancy(vol, cell=4),
+                                stats=s1)
+        assert torch.equal(a, b)
+        assert s1.tolist() == s2.tolist() and fallbacks == 0
+    go = torch.randn_like(plain)
+    full = raymarch_backward(go, vol, vol, M2, src2, tgt2, step2, n, 1, det, True, False)
+    skip = raymarch_backward(go, vol, vol, M2, src2, tgt2, step2, n, 1, det, True, False, windows=win)
+    assert rel_maxabs(skip[0], full[0]) < 1e-5
+
+
+def test_render_with_learned_proposal_through_autograd():
+    vol, net, n, det = _trained()
+    ph, sub, vol, lab, M, src, tgt, step, n, det, k_inv, sdd, rt = _case(B=3, seed=97)
+    rt1 = rt.clone().requires_grad_(True)
+    img = nd.render(sub, k_inv, rt1, sdd, det, det, n_samples=n)
+    w = torch.randn_like(img)
+    (img * w).sum().backward()
+    sub.empty_space = EmptySpace.proposal(vol, net, cell=4, margin=2.0)
+    rt2 = rt.clone().requires_grad_(True)
+    img2 = nd.render(sub, k_inv, rt2, sdd, det, det, n_samples=n)
+    (img2 * w).sum().backward()
+    assert rel_maxabs(img2, img) < 1e-6
+    assert rel_maxabs(rt2.grad, rt1.grad) < 1e-5

@@ -361,3 +361,45 @@ def test_brick_volume_gradient_matches_direct_and_oracle(C, cap, tile):
     ref = march_numpy_adjoint(np64(go), vol, lab, M, src, tgt, step, n, C)
     assert rel_maxabs(brick[0], ref[0]) < 1e-4
     assert rel_maxabs(brick[1], ref[1]) < 1e-3
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16, torch.float16])
+@pytest.mark.parametrize("C", [1, 4])
+def test_quad_layout_equals_plain_layout(dtype, C):
+    """The quad layout holds exact copies of the corners: forward and pose
+    gradient are bitwise equal to the plain layout's; the volume gradient
+    (different atomic order, folded from quad entries) agrees to rounding."""
+    from nanodrr_gb300.raymarch import quad_volume
+
+    n = 170
+    vol, lab, M, src, tgt, step, width = _random_case(31, B=2, Hd=21, Wd=27, C=C)
+    t = lambda a: torch.from_numpy(a).to(DEV)  # noqa: E731
+    v = t(vol).to(dtype)
+    q = quad_volume(v)
+    D, H, W = vol.shape
+    assert q.numel() == (D + 4) * (H + 3) * (W + 3) * (16 if dtype == torch.float32 else 8)
+    plain, _ = raymarch_forward(v, t(lab), t(M), t(src), t(tgt), t(step), n, C, width)
+    quad, _ = raymarch_forward(v, t(lab), t(M), t(src), t(tgt), t(step), n, C, width, quad=q)
+    assert torch.equal(plain, quad)
+    go = torch.randn(plain.shape, device=DEV)
+    gp = raymarch_backward(go, v, t(lab), t(M), t(src), t(tgt), t(step), n, C, width, True, True)
+    gq = raymarch_backward(go, v, t(lab), t(M), t(src), t(tgt), t(step), n, C, width, True, True, quad=q)
+    for a, b in zip(gp[1:], gq[1:]):  # gM, gsrc, gtgt, gstep
+        assert rel_maxabs(b, a) < 1e-6
+    assert rel_maxabs(gq[0], gp[0]) < 1e-5
+
+
+def test_render_uses_quad_layout_and_plain_on_request(random32):
+    g = random32
+    sub = subject_from_arrays(g["vol"], None, g["voxel_to_world"], 1)
+    k_inv, rt, sdd, H, W = rays_for(g)
+    out_q = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=200)
+    assert getattr(sub, "_ndrr_quad_cache", None) is not None
+    sub.layout = "plain"
+    out_p = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=200)
+    assert torch.equal(out_q, out_p)
+    # the cached quad follows in-place volume edits
+    sub.layout = "quad"
+    sub._image_hu.mul_(2.0)
+    out_2 = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=200)
+    assert rel_maxabs(out_2, 2 * out_q) < 1e-6
