@@ -178,7 +178,9 @@ typedef struct ndrr_raymarch_args {
     int32_t gvol_mode;      /* adjoint volume-gradient scatter: 0 auto,
                                1 direct global atomics per tap, 2 per-slab
                                shared-memory brick flushed with coalesced
-                               atomics (NDRR_GVOL_*)                            */
+                               atomics, 3 slab-ordered work (quad layout, no
+                               camera gradients; see NDRR_GVOL_SLAB)
+                               (NDRR_GVOL_*)                                    */
     int32_t reserved[4];
 } ndrr_raymarch_args;
 
@@ -188,10 +190,17 @@ enum ndrr_skip_mode {
     NDRR_SKIP_PROPOSAL = 2,
 };
 
+/* NDRR_GVOL_SLAB: the volume is cut into slabs of a few MB of gradient along
+ * one axis per pose, and (slab, pose, tile) work items run slab by slab
+ * across all poses, so that a slab's gradient lines are reused from L2 by
+ * every pose before eviction. Needs a larger workspace (work list and
+ * per-item pose partials: ndrr_raymarch_bwd_workspace_bytes reports it); gM
+ * stays deterministic (fixed partial slots and summation order). */
 enum ndrr_gvol_mode {
     NDRR_GVOL_AUTO = 0,
     NDRR_GVOL_DIRECT = 1,
     NDRR_GVOL_BRICK = 2,
+    NDRR_GVOL_SLAB = 3,
 };
 
 /* Library identity. */

@@ -69,6 +69,12 @@ cudaError_t launch_bwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaS
             e = cudaMemsetAsync(a.gvol_quad, 0, (size_t)(a.D + 4) * (a.H + 3) * (a.W + 3) * 16, st);
             if (e != cudaSuccess) return e;
         }
+        if (gvol && ls.slab) {
+            // slab-ordered adjoint: writes gM itself (ndrr_slab.cu)
+            e = launch_bwd_slab(a, ls, p, st);
+            if (e == cudaSuccess) e = launch_quad_fold(a.gvol_quad, a.D, a.H, a.W, a.gvol, st);
+            return e;
+        }
         e = launch_bwd_quad(p, a.vol_dtype, multi, gvol, gcam, skip, grid, block, bwd_smem_bytes(a, ls), st);
         if (e == cudaSuccess && gvol) e = launch_quad_fold(a.gvol_quad, a.D, a.H, a.W, a.gvol, st);
     } else if (gvol && ls.brick) {

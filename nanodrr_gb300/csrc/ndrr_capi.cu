@@ -101,8 +101,10 @@ int32_t validate_common(const ndrr_raymarch_args* a) {
         return fail(NDRR_ERR_INVALID_ARGUMENT, "sample_window and skip_mode are exclusive (one skip at a time)");
     if (a->vol_quad != nullptr && (long long)(a->D + 4) * (a->H + 3) * (a->W + 3) >= kInt32Max)
         return fail(NDRR_ERR_LIMIT, "quad layout of a %dx%dx%d volume exceeds int32 indexing", a->D, a->H, a->W);
-    if (a->gvol_mode < NDRR_GVOL_AUTO || a->gvol_mode > NDRR_GVOL_BRICK)
-        return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode must be 0, 1 or 2 (got %d)", a->gvol_mode);
+    if (a->gvol_mode < NDRR_GVOL_AUTO || a->gvol_mode > NDRR_GVOL_SLAB)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode must be 0, 1, 2 or 3 (got %d)", a->gvol_mode);
+    if (a->gvol_mode == NDRR_GVOL_SLAB && a->vol_quad == nullptr)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode 3 (slab-ordered) needs the quad layout (vol_quad)");
     if (a->reserved[0] < 0 || a->reserved[0] > 56 * 1024)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "brick capacity %d out of range [0, 57344] voxels", a->reserved[0]);
     return NDRR_OK;

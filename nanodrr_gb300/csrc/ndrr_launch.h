@@ -16,6 +16,7 @@ struct LaunchShape {
     int cap = 0;         // brick capacity in voxels
     int L0 = 16;         // initial slab length in samples
     int sm = 0;          // SM count of the device (0 when unknown)
+    bool slab = false;   // adjoint with volume gradient ordered slab by slab (quad layout)
 };
 
 LaunchShape choose_shape(const ndrr_raymarch_args& a, int sm_count);
@@ -28,6 +29,7 @@ size_t brick_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
 cudaError_t launch_fwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
 cudaError_t launch_skip_windows(const ndrr_raymarch_args& a, int32_t* windows, cudaStream_t st);
 cudaError_t launch_bwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
+uint64_t slab_workspace_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
 cudaError_t launch_batched(const ndrr_batch_args& a, bool backward, int sm_count, cudaStream_t st);
 cudaError_t launch_occupancy(const void* vol, int vol_dtype, int D, int H, int W, int cell, int max_dist,
                              uint8_t* dist, uint8_t* scratch, cudaStream_t st);

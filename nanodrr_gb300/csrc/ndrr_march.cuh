@@ -582,8 +582,65 @@ __device__ __forceinline__ void adjoint_epilogue(const MarchParams& p, const siz
 
 // Adjoint with direct global atomics for the volume gradient.
 // SKIP (only with GVOL false, see apply_skip): 0 none, 1 occupancy.
-template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP, bool QUAD = false>
-__device__ __forceinline__ void bwd_body(const MarchParams& p, const int tile, const int b, const size_t slot) {
+// Volume slab of the slab-ordered adjoint: only samples whose scatter cell
+// along `axis` (shifted by 2, see cell_index_shifted) lies in [c0, c1).
+struct SlabCut {
+    int axis;
+    int c0, c1;
+};
+
+// Cell index of the quad scatter along one axis (the clamp and floor of
+// quad_cell), shifted by 2 into [0, dim + 2].
+__device__ __forceinline__ int cell_index_shifted(const Ray& r, int axis, float t, int dim) {
+    const float p0 = axis == 0 ? r.p0x : (axis == 1 ? r.p0y : r.p0z);
+    const float d = axis == 0 ? r.dx : (axis == 1 ? r.dy : r.dz);
+    const float x = fminf(fmaxf(fmaf(t, d, p0), -2.0f), (float)dim + 1.0f);
+    return min((int)floorf(x), dim) + 2;
+}
+
+// First s in [lo, hi) whose cell index along the cut's axis is >= c (index
+// non-decreasing in s) or < c (non-increasing); hi when there is none. The
+// index is monotonic in s, so a binary search over the exact per-sample
+// computation finds the boundary.
+__device__ __forceinline__ int slab_bound(const Ray& r, const MarchParams& p, int axis, int dim, int lo, int hi,
+                                          int c, bool increasing) {
+    while (lo < hi) {
+        const int mid = lo + ((hi - lo) >> 1);
+        const int i = cell_index_shifted(r, axis, (float)mid * p.inv_s, dim);
+        if (increasing ? (i >= c) : (i < c))
+            hi = mid;
+        else
+            lo = mid + 1;
+    }
+    return lo;
+}
+
+// Restrict a ray's window to the samples of one slab.
+__device__ __forceinline__ void restrict_to_slab(const MarchParams& p, ThreadRay& tr, const SlabCut& cut) {
+    Ray& r = tr.ray;
+    if (r.lo >= r.hi) return;
+    const int dim = cut.axis == 0 ? p.W : (cut.axis == 1 ? p.H : p.D);
+    const float d = cut.axis == 0 ? r.dx : (cut.axis == 1 ? r.dy : r.dz);
+    int a, e;
+    if (d > 0.f) {
+        a = slab_bound(r, p, cut.axis, dim, r.lo, r.hi, cut.c0, true);
+        e = slab_bound(r, p, cut.axis, dim, a, r.hi, cut.c1, true);
+    } else if (d < 0.f) {
+        a = slab_bound(r, p, cut.axis, dim, r.lo, r.hi, cut.c1, false);
+        e = slab_bound(r, p, cut.axis, dim, a, r.hi, cut.c0, false);
+    } else {
+        const int i = cell_index_shifted(r, cut.axis, (float)r.lo * p.inv_s, dim);
+        const bool in = i >= cut.c0 && i < cut.c1;
+        a = r.lo;
+        e = in ? r.hi : r.lo;
+    }
+    r.lo = a;
+    r.hi = e;
+}
+
+template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP, bool QUAD = false, bool SLAB = false>
+__device__ __forceinline__ void bwd_body(const MarchParams& p, const int tile, const int b, const size_t slot,
+                                         const SlabCut cut = SlabCut{0, 0, 0}) {
     extern __shared__ float smem[];
     const int R = p.tw * p.th;
     const int NT = R * p.K;
@@ -600,6 +657,7 @@ __device__ __forceinline__ void bwd_body(const MarchParams& p, const int tile, c
         // Skipped samples have eight zero corners: no pose or camera terms.
         apply_skip(p, tr, 0.f, 1.f);
     }
+    if constexpr (SLAB) restrict_to_slab(p, tr, cut);
     chunk_thread_ray(tr, k, p.K);
     float go_ray = 0.f;
     if (!MULTI && n >= 0) go_ray = ld_any_f(p.go, p.go_dtype, tr.bn);
@@ -770,6 +828,8 @@ cudaError_t launch_quad_fold(const float* gquad, int D, int H, int W, float* gvo
 cudaError_t launch_quad_build(const void* vol, int dtype, int D, int H, int W, void* quad, cudaStream_t st);
 
 MarchParams make_params(const ndrr_raymarch_args& a, const LaunchShape& ls);
+cudaError_t launch_bwd_slab(const ndrr_raymarch_args& a, const LaunchShape& ls, const MarchParams& p,
+                            cudaStream_t st);
 size_t fwd_base_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
 
 template <typename Kern>

@@ -77,6 +77,8 @@ LaunchShape choose_shape(const ndrr_raymarch_args& a, int sm_count) {
     ls.brick = a.gvol_mode == NDRR_GVOL_BRICK;
     if (ls.tw * ls.th > 256) ls.brick = false;  // brick kernel is built for <= 256 threads
     if (a.vol_quad != nullptr) ls.brick = false;  // the quad layout has its own scatter
+    // Slab-ordered volume-gradient adjoint: quad layout, no camera gradients.
+    ls.slab = a.gvol_mode == NDRR_GVOL_SLAB && a.vol_quad != nullptr && a.need_gvol && !a.need_gcam;
     if (ls.brick) {
         ls.K = 1;
         const int nt = ls.tw * ls.th;
@@ -94,6 +96,7 @@ size_t brick_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls) {
 }
 
 uint64_t bwd_workspace_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls) {
+    if (ls.slab) return slab_workspace_bytes(a, ls);
     const TileMap tm = make_tilemap(a.N, a.width, ls.tw, ls.th);
     return (uint64_t)a.B * tm.tiles * kPartialStride * sizeof(float);
 }

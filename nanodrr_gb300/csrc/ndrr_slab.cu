@@ -1,0 +1,332 @@
+// Slab-ordered adjoint with volume gradient (quad layout).
+//
+// The volume-gradient adjoint is bound by read-modify-write traffic: each
+// pose's rays sweep the whole quad gradient (16 B per cell-plane corner
+// quad, 4x the volume), and by the time the next pose sweeps the same
+// region the previous sweep's lines have left the 126 MB L2, so every pose
+// pays a DRAM read and write of everything it touches. Here the volume is cut
+// into slabs along one axis per pose (the axis the pose's rays run most
+// nearly parallel to its planes, so that each ray crosses few slabs), each
+// slab a few MB of gradient, and the work is ordered slab by slab across ALL
+// poses: a work item is (slab, pose, detector tile), marching only the
+// samples whose scatter cell lies in the slab. Items of one slab run
+// together, so the slab's gradient (and volume) lines are reused from L2 by
+// every pose before they are evicted.
+//
+// Determinism of the pose gradient: every item writes its CTA partial to a
+// fixed slot (tile offset from a prefix sum + slab rank within the tile's
+// slab range), and the per-pose sum runs over tiles and slabs in a fixed
+// order, so gM does not depend on which CTA took which item when.
+//
+// Steps (one stream, no host synchronisation, capturable):
+//   slab_plan_kernel     per (pose, tile): the pose's axis and the tile's
+//                        slab range [k0, k1]; a histogram of items per slab
+//   slab_scan_kernel     prefix sums: tile offsets of the partial slots and
+//                        the start of each slab's items in the work list
+//   slab_fill_kernel     the work list, grouped by slab
+//   raymarch_bwd_slab_kernel  persistent CTAs take items from an atomic
+//                        counter in list order
+//   slab_pose_reduce_kernel   fixed-order per-pose sums of the partials
+#include "ndrr_march.cuh"
+
+namespace ndrr {
+
+// Workspace layout, computed identically on the host (sizes) and passed to
+// the kernels as pointers.
+struct SlabParams {
+    int Z[3];         // slab thickness in cells per axis (x, y, z)
+    int ns[3];        // slabs per axis
+    int base[3];      // first global slab id of each axis
+    int* counters;    // [0] items, [1] work counter
+    int* hist;        // [ns_total] items per global slab, then scanned cursors
+    int2* trange;     // [B * tiles] slab range of each tile (k0 > k1: none)
+    int* count;       // [B * tiles] items of each tile
+    int* offset;      // [B * tiles + 1] first partial slot of each tile
+    int* axis;        // [B] slab axis of each pose
+    int2* items;      // [max_items] (pose * tiles + tile, slab)
+    float* partials;  // [max_items][kPartialStride]
+    int ns_total;
+    int BT;
+};
+
+constexpr size_t kSlabTargetBytes = 24u << 20;  // quad gradient bytes per slab
+
+static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
+
+// Host-side slab geometry: thickness per axis so that a slab of the quad
+// gradient holds about kSlabTargetBytes (at least one cell).
+static void slab_geometry(const ndrr_raymarch_args& a, int Z[3], int ns[3]) {
+    const long long qx = a.W + 3, qy = a.H + 3, qz = a.D + 4;
+    const long long plane[3] = {qz * qy * 16, qz * qx * 16, qy * qx * 16};  // bytes per unit thickness
+    const int cells[3] = {a.W + 3, a.H + 3, a.D + 3};  // shifted cell indices 0 .. dim + 2
+    for (int i = 0; i < 3; ++i) {
+        Z[i] = (int)std::max<long long>(1, (long long)kSlabTargetBytes / std::max<long long>(plane[i], 1));
+        Z[i] = std::min(Z[i], cells[i]);
+        ns[i] = (cells[i] + Z[i] - 1) / Z[i];
+    }
+}
+
+struct SlabLayout {
+    size_t counters, hist, trange, count, offset, axis, items, partials, total;
+    long long max_items;
+};
+
+static SlabLayout slab_layout(const ndrr_raymarch_args& a, const LaunchShape& ls) {
+    int Z[3], ns[3];
+    slab_geometry(a, Z, ns);
+    const TileMap tm = make_tilemap(a.N, a.width, ls.tw, ls.th);
+    const long long BT = (long long)a.B * tm.tiles;
+    const int ns_total = ns[0] + ns[1] + ns[2];
+    const int ns_max = std::max(ns[0], std::max(ns[1], ns[2]));
+    SlabLayout L;
+    L.max_items = BT * ns_max;
+    size_t o = 0;
+    L.counters = o; o = align16(o + 4 * sizeof(int));
+    L.hist = o;     o = align16(o + (size_t)ns_total * sizeof(int));
+    L.trange = o;   o = align16(o + (size_t)BT * sizeof(int2));
+    L.count = o;    o = align16(o + (size_t)BT * sizeof(int));
+    L.offset = o;   o = align16(o + (size_t)(BT + 1) * sizeof(int));
+    L.axis = o;     o = align16(o + (size_t)a.B * sizeof(int));
+    L.items = o;    o = align16(o + (size_t)L.max_items * sizeof(int2));
+    L.partials = o; o = align16(o + (size_t)L.max_items * kPartialStride * sizeof(float));
+    L.total = o;
+    return L;
+}
+
+uint64_t slab_workspace_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls) {
+    return slab_layout(a, ls).total;
+}
+
+// Slab axis of a pose: the voxel axis along which the camera's optical axis
+// (third column of M) has the smallest component, ties to z then y.
+__device__ __forceinline__ int pose_slab_axis(const float (&m)[12]) {
+    const float ax = fabsf(m[2]), ay = fabsf(m[6]), az = fabsf(m[10]);
+    int axis = 2;
+    float best = az;
+    if (ay < best) { axis = 1; best = ay; }
+    if (ax < best) axis = 0;
+    return axis;
+}
+
+// ---------------------------------------------------------------- planning
+__global__ void __launch_bounds__(512) slab_plan_kernel(const MarchParams p, const SlabParams s) {
+    __shared__ int red[2];
+    const int R = p.tw * p.th;
+    const int bt = blockIdx.x;
+    const int b = bt / p.tm.tiles, tile = bt % p.tm.tiles;
+    float m[12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) m[j] = __ldg(p.M + (size_t)b * 12 + j);
+    const int axis = pose_slab_axis(m);
+    if (threadIdx.x == 0) {
+        red[0] = INT_MAX;
+        red[1] = -1;
+        if (tile == 0) s.axis[b] = axis;
+    }
+    __syncthreads();
+    if ((int)threadIdx.x < R) {
+        const int n = tile_ray(p.tm, p.N, p.tw, p.th, tile, threadIdx.x);
+        ThreadRay tr;
+        init_thread_ray(p, m, b, n, tr);
+        if (n >= 0 && tr.ray.lo < tr.ray.hi) {
+            const int dim = axis == 0 ? p.W : (axis == 1 ? p.H : p.D);
+            const int i0 = cell_index_shifted(tr.ray, axis, (float)tr.ray.lo * p.inv_s, dim);
+            const int i1 = cell_index_shifted(tr.ray, axis, (float)(tr.ray.hi - 1) * p.inv_s, dim);
+            atomicMin(&red[0], min(i0, i1) / s.Z[axis]);
+            atomicMax(&red[1], max(i0, i1) / s.Z[axis]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const int k0 = red[0], k1 = red[1];
+        if (k1 >= 0) {
+            s.trange[bt] = make_int2(k0, k1);
+            s.count[bt] = k1 - k0 + 1;
+            for (int k = k0; k <= k1; ++k) atomicAdd(&s.hist[s.base[axis] + k], 1);
+        } else {
+            s.trange[bt] = make_int2(1, 0);
+            s.count[bt] = 0;
+        }
+    }
+}
+
+// Exclusive scan of n ints in place (one CTA), returning the total.
+__device__ int block_exclusive_scan(int* v, int n, int* sh) {
+    const int T = blockDim.x, tid = threadIdx.x;
+    const int per = (n + T - 1) / T;
+    const int beg = min(n, tid * per), end = min(n, beg + per);
+    int sum = 0;
+    for (int i = beg; i < end; ++i) sum += v[i];
+    sh[tid] = sum;
+    __syncthreads();
+    // Hillis-Steele over the per-thread sums
+    for (int o = 1; o < T; o <<= 1) {
+        const int x = tid >= o ? sh[tid - o] : 0;
+        __syncthreads();
+        sh[tid] += x;
+        __syncthreads();
+    }
+    int run = sh[tid] - sum;  // exclusive prefix of this thread's chunk
+    for (int i = beg; i < end; ++i) {
+        const int c = v[i];
+        v[i] = run;
+        run += c;
+    }
+    const int total = sh[T - 1];
+    __syncthreads();
+    return total;
+}
+
+__global__ void __launch_bounds__(1024) slab_scan_kernel(const SlabParams s) {
+    __shared__ int sh[1024];
+    // tile offsets: offset[bt] = sum of count over earlier tiles
+    for (int i = threadIdx.x; i < s.BT; i += blockDim.x) s.offset[i] = s.count[i];
+    __syncthreads();
+    const int items = block_exclusive_scan(s.offset, s.BT, sh);
+    if (threadIdx.x == 0) s.offset[s.BT] = items;
+    // slab cursors: start of each slab's items in the list
+    block_exclusive_scan(s.hist, s.ns_total, sh);
+    if (threadIdx.x == 0) {
+        s.counters[0] = items;
+        s.counters[1] = 0;
+    }
+}
+
+__global__ void __launch_bounds__(256) slab_fill_kernel(const SlabParams s, int tiles) {
+    const int bt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (bt >= s.BT) return;
+    const int2 r = s.trange[bt];
+    if (r.x > r.y) return;
+    const int axis = s.axis[bt / tiles];
+    for (int k = r.x; k <= r.y; ++k) {
+        const int pos = atomicAdd(&s.hist[s.base[axis] + k], 1);
+        s.items[pos] = make_int2(bt, k);
+    }
+}
+
+// ------------------------------------------------------------- the adjoint
+template <typename VT, bool MULTI>
+__global__ void __launch_bounds__(512, 1) raymarch_bwd_slab_kernel(const MarchParams p, const SlabParams s) {
+    __shared__ int item_sh;
+    const int total = s.counters[0];
+    while (true) {
+        __syncthreads();  // the previous item is done with item_sh and shared memory
+        if (threadIdx.x == 0) item_sh = atomicAdd(&s.counters[1], 1);
+        __syncthreads();
+        const int item = item_sh;
+        if (item >= total) break;
+        const int2 it = s.items[item];
+        const int bt = it.x, k = it.y;
+        const int b = bt / p.tm.tiles, tile = bt % p.tm.tiles;
+        const int axis = s.axis[b];
+        const SlabCut cut{axis, k * s.Z[axis], (k + 1) * s.Z[axis]};
+        const size_t slot = (size_t)s.offset[bt] + (size_t)(k - s.trange[bt].x);
+        bwd_body<VT, MULTI, true, false, 0, true, true>(p, tile, b, slot, cut);
+    }
+}
+
+// Per-pose fixed-order sum of the item partials: thread j of the CTA takes
+// tiles j, j + 256, ... in order and each tile's slabs in order.
+__global__ void __launch_bounds__(256) slab_pose_reduce_kernel(const SlabParams s, int tiles, float* __restrict__ gM) {
+    __shared__ float red[8][12];
+    const int b = blockIdx.x;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    float acc[12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) acc[j] = 0.f;
+    for (int t = tid; t < tiles; t += blockDim.x) {
+        const int bt = b * tiles + t;
+        const int n = s.count[bt];
+        const float* pp = s.partials + (size_t)s.offset[bt] * kPartialStride;
+        for (int q = 0; q < n; ++q) {
+#pragma unroll
+            for (int j = 0; j < 12; ++j) acc[j] += pp[(size_t)q * kPartialStride + j];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < 12; ++j) {
+        const float v = warp_sum(acc[j]);
+        if (lane == 0) red[warp][j] = v;
+    }
+    __syncthreads();
+    if (tid < 12) {
+        float sum = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) sum += red[w][tid];
+        gM[(size_t)b * 12 + tid] = sum;
+    }
+}
+
+template <typename VT, bool MULTI>
+static cudaError_t launch_slab_march(const MarchParams& p, const SlabParams& s, unsigned block, size_t smem,
+                                     cudaStream_t st) {
+    auto kern = raymarch_bwd_slab_kernel<VT, MULTI>;
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (int)block, smem);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = (unsigned)std::max(1, sms * std::max(per_sm, 1));
+    kern<<<grid, block, smem, st>>>(p, s);
+    return cudaGetLastError();
+}
+
+// Slab-ordered adjoint with volume gradient for the quad layout; writes gM
+// and scatters into p.gquad (zeroed by the caller, folded afterwards).
+cudaError_t launch_bwd_slab(const ndrr_raymarch_args& a, const LaunchShape& ls, const MarchParams& p0,
+                            cudaStream_t st) {
+    MarchParams p = p0;
+    const SlabLayout L = slab_layout(a, ls);
+    unsigned char* ws = reinterpret_cast<unsigned char*>(a.workspace);
+    SlabParams s;
+    slab_geometry(a, s.Z, s.ns);
+    s.base[0] = 0;
+    s.base[1] = s.ns[0];
+    s.base[2] = s.ns[0] + s.ns[1];
+    s.ns_total = s.ns[0] + s.ns[1] + s.ns[2];
+    s.BT = a.B * p.tm.tiles;
+    s.counters = reinterpret_cast<int*>(ws + L.counters);
+    s.hist = reinterpret_cast<int*>(ws + L.hist);
+    s.trange = reinterpret_cast<int2*>(ws + L.trange);
+    s.count = reinterpret_cast<int*>(ws + L.count);
+    s.offset = reinterpret_cast<int*>(ws + L.offset);
+    s.axis = reinterpret_cast<int*>(ws + L.axis);
+    s.items = reinterpret_cast<int2*>(ws + L.items);
+    s.partials = reinterpret_cast<float*>(ws + L.partials);
+    p.partials = s.partials;
+    p.K = 1;  // items are short: one thread per ray
+
+    cudaError_t e = cudaMemsetAsync(s.hist, 0, (size_t)s.ns_total * sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    const int R = p.tw * p.th;
+    slab_plan_kernel<<<s.BT, R, 0, st>>>(p, s);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    slab_scan_kernel<<<1, 1024, 0, st>>>(s);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    slab_fill_kernel<<<(s.BT + 255) / 256, 256, 0, st>>>(s, p.tm.tiles);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    const size_t smem = bwd_epilogue_bytes(a, ls);
+    const bool multi = a.n_classes > 1;
+    switch (a.vol_dtype) {
+        case NDRR_F32:
+            e = multi ? launch_slab_march<float, true>(p, s, R, smem, st) : launch_slab_march<float, false>(p, s, R, smem, st);
+            break;
+        case NDRR_F16:
+            e = multi ? launch_slab_march<__half, true>(p, s, R, smem, st)
+                      : launch_slab_march<__half, false>(p, s, R, smem, st);
+            break;
+        case NDRR_BF16:
+            e = multi ? launch_slab_march<__nv_bfloat16, true>(p, s, R, smem, st)
+                      : launch_slab_march<__nv_bfloat16, false>(p, s, R, smem, st);
+            break;
+        default: return cudaErrorInvalidValue;
+    }
+    if (e != cudaSuccess) return e;
+    slab_pose_reduce_kernel<<<a.B, 256, 0, st>>>(s, p.tm.tiles, a.gM);
+    return cudaGetLastError();
+}
+
+}  // namespace ndrr
