@@ -39,6 +39,9 @@ sys.path.insert(0, str(ROOT))
 import torch  # noqa: E402
 
 BASELINE_HEADLINE = None  # the benchmark spec publishes no number for this metric
+# DRAM read + write bytes per sample of the slab-ordered adjoint kernel from
+# an ncu capture (profiles/raymarch_bwd_slab_kernel_quad_gvol_f32_384cube_8poses.md)
+SLAB_DRAM_BYTES_PER_SAMPLE = 31.66
 
 
 def parse_args():
@@ -331,22 +334,26 @@ def run_ours(args, world, rank, local):
         quad = cached_quad(sub, vol)
         reps = max(3, args.steps)
         times = {"fwd": [], "fwd_learned": [], "bwd": [], "fwd_plain_layout": [], "bwd_plain_layout": [],
-                 "learned_windows": []}
+                 "learned_windows": [], "bwd_direct": []}
         for i in range(reps + 1):
-            e = [torch.cuda.Event(enable_timing=True) for _ in range(8)]
+            e = [torch.cuda.Event(enable_timing=True) for _ in range(9)]
             e[0].record()
             raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, quad=quad)
             e[1].record()
             raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, skip=skips["learned"], quad=quad)
             e[2].record()
-            raymarch_backward(go, vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, True, True, gvol=gvol, quad=quad)
+            # the step's adjoint: pose + volume gradient (slab-ordered, quad layout)
+            raymarch_backward(go, vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, True, False, gvol=gvol, quad=quad)
             e[3].record()
             raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd)
             e[4].record()
-            raymarch_backward(go, vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, True, True, gvol=gvol)
+            raymarch_backward(go, vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, True, False, gvol=gvol)
             e[5].record()
             skip_windows(vol, M, srcb, tgtb, stepsz, S, Hd, skips["learned"])
             e[6].record()
+            raymarch_backward(go, vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, True, False, gvol=gvol, quad=quad,
+                              gvol_mode=1)
+            e[7].record()
             torch.cuda.synchronize()
             if i > 0:
                 times["fwd"].append(e[0].elapsed_time(e[1]))
@@ -355,6 +362,7 @@ def run_ours(args, world, rank, local):
                 times["fwd_plain_layout"].append(e[3].elapsed_time(e[4]))
                 times["bwd_plain_layout"].append(e[4].elapsed_time(e[5]))
                 times["learned_windows"].append(e[5].elapsed_time(e[6]))
+                times["bwd_direct"].append(e[6].elapsed_time(e[7]))
     e_bytes = vol.element_size()
     fwd_bytes = n_samp * 8 * e_bytes
     bwd_bytes = n_samp * (8 * e_bytes + 4 + 8 * 4 * 2)
@@ -367,13 +375,17 @@ def run_ours(args, world, rank, local):
     ost = occ_stats.tolist()
     roofline = {
         "bound": "hbm",
-        "kernel": "raymarch_bwd_kernel (adjoint with volume gradient, quad layout)",
+        "kernel": "raymarch_bwd_slab_kernel (adjoint with pose and volume gradient, slab-ordered, quad layout)",
+        "timed": "the whole adjoint call on its stream: gradient memset, slab plan, kernel, pose reduction, fold",
         "achieved": round(achieved, 1),
         "peak": peaks["hbm_gbs"],
         "peak_source": peaks["source"],
         "unit": "GB/s",
         "frac": round(achieved / peaks["hbm_gbs"], 4),
-        "traffic": None,
+        # DRAM bytes of the kernel per sample from the ncu capture of the
+        # 384^3 x 8-pose case, scaled by this launch's samples
+        "traffic": round(SLAB_DRAM_BYTES_PER_SAMPLE * n_samp, 1) if SLAB_DRAM_BYTES_PER_SAMPLE else None,
+        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, 384^3 x 8 poses, scaled per sample",
         "algorithmic_bytes_per_launch": bwd_bytes,
         "samples_per_launch": n_samp,
         "fwd_ms": round(fwd_s * 1e3, 3),
@@ -385,6 +397,7 @@ def run_ours(args, world, rank, local):
         "fwd_frac_of_hbm": round(fwd_bytes / fwd_s / 1e9 / peaks["hbm_gbs"], 4),
         "plain_layout_fwd_ms": round(statistics.median(times["fwd_plain_layout"]), 3),
         "plain_layout_bwd_ms": round(statistics.median(times["bwd_plain_layout"]), 3),
+        "direct_scatter_bwd_ms": round(statistics.median(times["bwd_direct"]), 3),
     }
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -438,9 +451,9 @@ def run_ours(args, world, rank, local):
         "samples_per_s": round(n_samp * args.steps * world / t_dev, 1),
         "roofline": roofline,
         "e2e": e2e,
-        # per step: [window kernel (learned)], forward march, adjoint march,
-        # quad-gradient fold, per-pose reduction of the pose partials
-        "gpu_launches": (5 if headline == "learned" else 4) * args.steps,
+        # per step: [window kernel (learned)], forward march, slab plan, scan
+        # and fill, adjoint march, per-pose reduction, quad-gradient fold
+        "gpu_launches": (8 if headline == "learned" else 7) * args.steps,
         "clocks": clk,
     }
     if cpu is not None:

@@ -181,7 +181,11 @@ typedef struct ndrr_raymarch_args {
                                atomics, 3 slab-ordered work (quad layout, no
                                camera gradients; see NDRR_GVOL_SLAB)
                                (NDRR_GVOL_*)                                    */
-    int32_t reserved[4];
+    int32_t brick_cap;      /* gvol_mode 2: brick capacity in voxels (0 default,
+                               at most 57344)                                   */
+    int32_t slab_mib;       /* gvol_mode 3 (and auto): quad-gradient MiB per
+                               slab (0 default = 96, at most 4096)              */
+    int32_t reserved[2];
 } ndrr_raymarch_args;
 
 enum ndrr_skip_mode {
@@ -190,12 +194,14 @@ enum ndrr_skip_mode {
     NDRR_SKIP_PROPOSAL = 2,
 };
 
-/* NDRR_GVOL_SLAB: the volume is cut into slabs of a few MB of gradient along
- * one axis per pose, and (slab, pose, tile) work items run slab by slab
- * across all poses, so that a slab's gradient lines are reused from L2 by
- * every pose before eviction. Needs a larger workspace (work list and
- * per-item pose partials: ndrr_raymarch_bwd_workspace_bytes reports it); gM
- * stays deterministic (fixed partial slots and summation order). */
+/* NDRR_GVOL_SLAB: the volume is cut into slabs (about 96 MB of quad
+ * gradient each) along one axis per pose, and (slab, pose, tile) work items
+ * run slab by slab across all poses, so that a slab's lines are reused from
+ * L2 by every pose before eviction. It is what NDRR_GVOL_AUTO selects for
+ * the quad layout without camera gradients. Needs a larger workspace (work
+ * list and per-item pose partials: ndrr_raymarch_bwd_workspace_bytes
+ * reports it); gM stays deterministic (fixed partial slots and summation
+ * order). */
 enum ndrr_gvol_mode {
     NDRR_GVOL_AUTO = 0,
     NDRR_GVOL_DIRECT = 1,

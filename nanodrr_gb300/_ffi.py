@@ -88,7 +88,9 @@ class RaymarchArgs(ctypes.Structure):
         ("tile_h", ctypes.c_int32),
         ("sample_split", ctypes.c_int32),
         ("gvol_mode", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 4),
+        ("brick_cap", ctypes.c_int32),
+        ("slab_mib", ctypes.c_int32),
+        ("reserved", ctypes.c_int32 * 2),
     ]
 
     def __init__(self, **kw):

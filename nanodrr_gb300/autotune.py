@@ -2,10 +2,11 @@
 
 The reference uses fixed tiling constants (nanodrr src/nanodrr/drr/_fused.py:
 5-7) and a split heuristic (`_split`, :341-346). Here the tile shape and the
-in-CTA sample split are picked per request class by timing candidates on the
-caller's own rays with CUDA events, and cached (in memory and, when a path is
-given, in a JSON file) under a key of volume shape, dtype, detector, sample
-count, classes and batch size.
+in-CTA sample split, and the slab size of the slab-ordered volume-gradient
+adjoint, are picked per request class by timing candidates on the caller's
+own rays with CUDA events, and cached (in memory and, when a path is given,
+in a JSON file) under a key of volume shape, dtype, detector, sample count,
+classes and batch size.
 """
 
 from __future__ import annotations
@@ -17,12 +18,14 @@ from pathlib import Path
 
 import torch
 
-from .raymarch import raymarch_forward
+from .raymarch import raymarch_backward, raymarch_forward
 
 # (tile_w, tile_h, sample_split) with 256 threads: the batched kernel's shapes.
 BATCHED_CANDIDATES = [(16, 16, 1), (16, 8, 2), (8, 8, 4), (32, 8, 1)]
 # shapes for the single-request kernels (up to 512 threads)
 SINGLE_CANDIDATES = [(16, 8, 1), (16, 16, 1), (32, 8, 1), (16, 8, 2), (8, 8, 4), (16, 8, 4)]
+# quad-gradient MiB per slab for the slab-ordered volume-gradient adjoint
+SLAB_CANDIDATES = [48, 96, 192]
 
 
 class Autotuner:
@@ -71,6 +74,29 @@ class Autotuner:
         self.cache[k] = list(best)
         self.save()
         return best
+
+    def best_slab_mib(self, vol, quad, M, src, tgt, step, n_samples, width, n_classes=1, lab=None,
+                      candidates=SLAB_CANDIDATES) -> int:
+        """Fastest slab size (MiB of quad gradient) for the slab-ordered
+        adjoint with volume gradient on these rays (cached); set it as
+        `subject.slab_mib` for `render`."""
+        B, N, _ = tgt.shape
+        k = "slab:" + self.key(vol, n_classes, B, N, width, n_samples, None)
+        if k in self.cache:
+            return int(self.cache[k][0])
+        lab = vol if lab is None else lab
+        go = torch.ones(B, n_classes, N, device=vol.device)
+        gvol = torch.zeros(vol.shape, device=vol.device)
+        timings = {}
+        for mib in candidates:
+            timings[mib] = self._time(
+                lambda: raymarch_backward(go, vol, lab, M, src, tgt, step, n_samples, n_classes, width, True, False,
+                                          gvol=gvol, quad=quad, gvol_mode=3, slab_mib=mib)
+            )
+        best = min(timings, key=timings.get)
+        self.cache[k] = [int(best)]
+        self.save()
+        return int(best)
 
     def save(self) -> None:
         if self.path is None:

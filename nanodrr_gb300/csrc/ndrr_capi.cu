@@ -105,8 +105,10 @@ int32_t validate_common(const ndrr_raymarch_args* a) {
         return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode must be 0, 1, 2 or 3 (got %d)", a->gvol_mode);
     if (a->gvol_mode == NDRR_GVOL_SLAB && a->vol_quad == nullptr)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode 3 (slab-ordered) needs the quad layout (vol_quad)");
-    if (a->reserved[0] < 0 || a->reserved[0] > 56 * 1024)
-        return fail(NDRR_ERR_INVALID_ARGUMENT, "brick capacity %d out of range [0, 57344] voxels", a->reserved[0]);
+    if (a->brick_cap < 0 || a->brick_cap > 56 * 1024)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "brick capacity %d out of range [0, 57344] voxels", a->brick_cap);
+    if (a->slab_mib < 0 || a->slab_mib > 4096)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "slab size %d MiB out of range [0, 4096]", a->slab_mib);
     return NDRR_OK;
 }
 
@@ -368,17 +370,20 @@ extern "C" int32_t ndrr_raymarch_bwd_noalloc(const ndrr_raymarch_args* a, void* 
     int32_t rc = validate_common(a);
     if (rc != NDRR_OK) return rc;
     if (a->B == 0 || a->N == 0) return ok();
-    const uint64_t need = ndrr::bwd_workspace_bytes(*a, ndrr::choose_shape(*a, 0));
+    // The automatic volume-gradient mode would pick the slab-ordered adjoint,
+    // whose work list does not fit the fixed scratch: use direct scatter.
+    ndrr_raymarch_args local = *a;
+    if (local.gvol_mode == NDRR_GVOL_AUTO) local.gvol_mode = NDRR_GVOL_DIRECT;
+    const uint64_t need = ndrr::bwd_workspace_bytes(local, ndrr::choose_shape(local, 0));
     if (need > kNoAllocScratchBytes)
         return fail(NDRR_ERR_LIMIT,
                     "the allocation-free adjoint holds %llu bytes of scratch but this call needs %llu "
-                    "(16 floats per pose and detector tile); use fewer poses per call, a larger tile, or "
-                    "ndrr_raymarch_bwd with a caller-provided workspace",
+                    "(16 floats per pose and detector tile, more with gvol_mode 3); use fewer poses per call, "
+                    "a larger tile, or ndrr_raymarch_bwd with a caller-provided workspace",
                     (unsigned long long)kNoAllocScratchBytes, (unsigned long long)need);
     void* scratch = nullptr;
     const cudaError_t e = noalloc_scratch(&scratch);
     if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "scratch address lookup failed: %s", cudaGetErrorString(e));
-    ndrr_raymarch_args local = *a;
     local.workspace = scratch;
     local.workspace_bytes = kNoAllocScratchBytes;
     return ndrr_raymarch_bwd(&local, stream);

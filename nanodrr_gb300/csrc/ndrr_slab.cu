@@ -7,7 +7,7 @@
 // pays a DRAM read and write of everything it touches. Here the volume is cut
 // into slabs along one axis per pose (the axis the pose's rays run most
 // nearly parallel to its planes, so that each ray crosses few slabs), each
-// slab a few MB of gradient, and the work is ordered slab by slab across ALL
+// slab about 96 MB of quad gradient, and the work is ordered slab by slab across ALL
 // poses: a work item is (slab, pose, detector tile), marching only the
 // samples whose scatter cell lies in the slab. Items of one slab run
 // together, so the slab's gradient (and volume) lines are reused from L2 by
@@ -49,18 +49,23 @@ struct SlabParams {
     int BT;
 };
 
-constexpr size_t kSlabTargetBytes = 24u << 20;  // quad gradient bytes per slab
+// Quad-gradient bytes per slab. Measured at 512^3 x 32 poses (adjoint ms):
+// 4 MiB 20.5, 8 MiB 20.5, 24 MiB 11.1, 48 MiB 9.8, 96 MiB 9.4, 192 MiB 10.2,
+// 384 MiB 11.0, direct scatter 10.3-10.6: thin slabs multiply the work items
+// (each ray is cut once per slab crossed), thick ones lose the L2 reuse.
+constexpr size_t kSlabTargetBytes = 96u << 20;  // default; args.slab_mib overrides
 
 static size_t align16(size_t x) { return (x + 15) & ~(size_t)15; }
 
 // Host-side slab geometry: thickness per axis so that a slab of the quad
-// gradient holds about kSlabTargetBytes (at least one cell).
+// gradient holds about the target bytes (at least one cell).
 static void slab_geometry(const ndrr_raymarch_args& a, int Z[3], int ns[3]) {
+    const long long target = a.slab_mib > 0 ? (long long)a.slab_mib << 20 : (long long)kSlabTargetBytes;
     const long long qx = a.W + 3, qy = a.H + 3, qz = a.D + 4;
     const long long plane[3] = {qz * qy * 16, qz * qx * 16, qy * qx * 16};  // bytes per unit thickness
     const int cells[3] = {a.W + 3, a.H + 3, a.D + 3};  // shifted cell indices 0 .. dim + 2
     for (int i = 0; i < 3; ++i) {
-        Z[i] = (int)std::max<long long>(1, (long long)kSlabTargetBytes / std::max<long long>(plane[i], 1));
+        Z[i] = (int)std::max<long long>(1, target / std::max<long long>(plane[i], 1));
         Z[i] = std::min(Z[i], cells[i]);
         ns[i] = (cells[i] + Z[i] - 1) / Z[i];
     }

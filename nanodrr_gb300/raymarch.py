@@ -280,6 +280,7 @@ def raymarch_backward(
     gvol: torch.Tensor | None = None,
     gvol_mode: int = 0,
     brick_cap: int = 0,
+    slab_mib: int = 0,
     tile: tuple[int, int, int] | None = None,
     skip=None,
     quad: torch.Tensor | None = None,
@@ -290,7 +291,9 @@ def raymarch_backward(
     `gvol`, when given, is a float32 [D, H, W] buffer the volume gradient is
     accumulated into (so several calls can share one); otherwise a zeroed one
     is allocated. `gvol_mode` selects the volume-gradient scatter (0 auto,
-    1 direct atomics, 2 per-slab shared-memory brick), `brick_cap` the brick
+    1 direct atomics, 2 per-slab shared-memory brick, 3 slab-ordered work,
+    which auto picks for the quad layout without camera gradients),
+    `slab_mib` the quad-gradient MiB per slab (0 = default), `brick_cap` the brick
     capacity in voxels (0 = default) and `tile` an explicit
     (tile_w, tile_h, sample_split) launch shape. Skips and `windows` apply to
     the pose/camera adjoint only: with `need_gvol` every sample is marched."""
@@ -339,7 +342,8 @@ def raymarch_backward(
         t_window = t_window.float().contiguous()
         a.t_window = _ptr(t_window)
     a.gvol_mode = int(gvol_mode)
-    a.reserved[0] = int(brick_cap)
+    a.brick_cap = int(brick_cap)
+    a.slab_mib = int(slab_mib)
     _apply_skip(a, skip, vol)
     if windows is not None:
         a.sample_window = _ptr(windows)
@@ -498,10 +502,12 @@ def fused_raymarch_ex(
     skip_mode: int,
     margin: float,
     windows_ahead: bool,
+    slab_mib: int,
 ) -> tuple[torch.Tensor, torch.Tensor]:
     """Returns (out [B, C, N], windows): with `windows_ahead` and a skip, the
     per-ray sample windows [B, N, 2] int32 the forward used, which the
-    pose/camera adjoint reuses; otherwise an empty int32 tensor."""
+    pose/camera adjoint reuses; otherwise an empty int32 tensor. `slab_mib`
+    is the adjoint's slab size (0 = default), passed through to it."""
     skip = _skip_of(vol, occ_grid, occ_cell, proposal, skip_mode, margin)
     windows = None
     if skip is not None and (windows_ahead or _windows_route(skip)):
@@ -516,7 +522,7 @@ def fused_raymarch_ex(
 
 @fused_raymarch_ex.register_fake
 def _(vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell, proposal, skip_mode,
-      margin, windows_ahead):
+      margin, windows_ahead, slab_mib):
     B, N, _ = tgt.shape
     out = torch.empty(B, n_classes, N, device=vol.device, dtype=vol.dtype)
     ahead = skip_mode == _ffi.NDRR_SKIP_PROPOSAL or (skip_mode != 0 and windows_ahead)
@@ -545,6 +551,7 @@ def fused_raymarch_ex_bwd(
     skip_mode: int,
     margin: float,
     windows: torch.Tensor,
+    slab_mib: int,
 ) -> tuple[torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor, torch.Tensor]:
     if need_gvol and torch.are_deterministic_algorithms_enabled():
         raise RuntimeError(
@@ -557,7 +564,7 @@ def fused_raymarch_ex_bwd(
         skip, win = _skip_of(vol, occ_grid, occ_cell, proposal, skip_mode, margin), None
     return raymarch_backward(
         go, vol, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam, skip=skip, quad=quad,
-        windows=win,
+        windows=win, slab_mib=slab_mib,
     )
 
 
@@ -575,19 +582,19 @@ def _(go, vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, need_g
 
 def _ex_setup_context(ctx, inputs, output):
     (vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell, proposal, mode,
-     margin, windows_ahead) = inputs
+     margin, windows_ahead, slab_mib) = inputs
     ctx.save_for_backward(vol, quad, lab, M.contiguous(), src, tgt, step, occ_grid, proposal, output[1])
-    ctx.args = (n_samples, n_classes, width, occ_cell, mode, margin)
+    ctx.args = (n_samples, n_classes, width, occ_cell, mode, margin, slab_mib)
 
 
 def _ex_backward(ctx, go, _gwin):
     vol, quad, lab, M, src, tgt, step, occ_grid, proposal, windows = ctx.saved_tensors
-    n_samples, n_classes, width, occ_cell, mode, margin = ctx.args
+    n_samples, n_classes, width, occ_cell, mode, margin, slab_mib = ctx.args
     need_gvol = ctx.needs_input_grad[0]
     need_gcam = any(ctx.needs_input_grad[i] for i in (4, 5, 6))
     gvol, gM, gsrc, gtgt, gstep = fused_raymarch_ex_bwd(
         go, vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam,
-        occ_grid, occ_cell, proposal, mode, margin, windows,
+        occ_grid, occ_cell, proposal, mode, margin, windows, slab_mib,
     )
     return (
         gvol.to(vol.dtype) if need_gvol else None,
@@ -597,7 +604,7 @@ def _ex_backward(ctx, go, _gwin):
         gsrc.to(src.dtype) if need_gcam else None,
         gtgt.to(tgt.dtype) if need_gcam else None,
         gstep.to(step.dtype) if need_gcam else None,
-        None, None, None, None, None, None, None, None, None,
+        None, None, None, None, None, None, None, None, None, None,
     )
 
 

@@ -116,7 +116,8 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
                   not getattr(skip, "fused", True))
         else:
             sk = (empty, 0, empty, 0, 0.0, False)
-        out = fused_raymarch_ex(args[0], quad, *args[1:], *sk)[0]
+        slab_mib = int(getattr(subject, "slab_mib", 0))
+        out = fused_raymarch_ex(args[0], quad, *args[1:], *sk, slab_mib)[0]
     return out.reshape(B, C, height, width)
 
 

@@ -101,3 +101,38 @@ def test_autotuner_picks_and_caches_a_valid_shape(tmp_path):
     assert (tmp_path / "tune.json").exists()
     again = Autotuner(tmp_path / "tune.json")
     assert len(again.cache) >= 1
+
+
+def test_autotuner_picks_a_slab_size_and_render_uses_it(tmp_path):
+    import nanodrr_gb300 as nd
+    from nanodrr_gb300.autotune import SLAB_CANDIDATES
+    from nanodrr_gb300.raymarch import quad_volume
+    from nanodrr_gb300.renderer import _affine_product, _make_src, _make_tgt
+
+    sub = phantom.make_phantom((40, 36, 44), (3.0, 3.0, 3.0), seed=4).subject(device=DEV)
+    vol = sub.image[0, 0].contiguous()
+    k_inv, sdd = phantom.detector(pixel=4.0, height=24, width=24)
+    k_inv, sdd = k_inv.to(DEV), sdd.to(DEV)
+    rt = phantom.random_poses(3, seed=6).to(DEV)
+    tgt = _make_tgt(k_inv, sdd, 24, 24, DEV, torch.float32).expand(3, -1, -1).contiguous()
+    src = _make_src(False, tgt, sdd.expand(3)).contiguous()
+    step = ((tgt - src).norm(dim=-1) / 149).contiguous()
+    M = _affine_product(sub.world_to_voxel[:3], rt).contiguous()
+    tuner = Autotuner(tmp_path / "tune.json", reps=2)
+    # tiny slabs (1 MiB) so that the work splits across many slabs here
+    mib = tuner.best_slab_mib(vol, quad_volume(vol), M, src, tgt, step, 150, 24, candidates=[1, 2, 96])
+    assert mib in (1, 2, 96)
+    assert Autotuner(tmp_path / "tune.json").best_slab_mib(vol, None, M, src, tgt, step, 150, 24,
+                                                           candidates=[1, 2, 96]) == mib  # cached
+    assert SLAB_CANDIDATES
+    # render with a volume gradient: slab size 1 MiB equals the default
+    vol_param = sub._image_hu.detach().clone().requires_grad_(True)
+    sub._image_hu = vol_param
+    w = torch.randn(3, 1, 24, 24, device=DEV)
+    (nd.render(sub, k_inv, rt, sdd, 24, 24, n_samples=150) * w).sum().backward()
+    g_default = vol_param.grad.clone()
+    vol_param.grad = None
+    sub.slab_mib = 1
+    (nd.render(sub, k_inv, rt, sdd, 24, 24, n_samples=150) * w).sum().backward()
+    rel = float((vol_param.grad - g_default).abs().max() / g_default.abs().max())
+    assert rel < 1e-5
