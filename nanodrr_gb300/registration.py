@@ -7,7 +7,8 @@ volume's isocenter, pose = rt_inv @ pivot @ T(rot, xyz) @ pivot^-1.
 `NormalizedCrossCorrelation2d` mirrors src/nanodrr/metrics/ncc.py:8-37
 (per-image zero-mean, unit-variance correlation, optional patches).
 Both are host-side torch: the heavy part of a registration step is the
-render and its adjoint, which run in the CUDA kernels.
+render and its adjoint, which run in the CUDA kernels. `GraphedStep` replays
+a whole step (pose, render, loss, backward) from a CUDA graph.
 """
 
 from __future__ import annotations
@@ -84,3 +85,54 @@ def _to_patches(x: torch.Tensor, p: int) -> torch.Tensor:
     x = x.unfold(2, p, step=1).unfold(3, p, step=1).contiguous()
     b, c, h, w, p1, p2 = x.shape
     return x.reshape(b, c * h * w, p1, p2)
+
+
+class GraphedStep:
+    """One registration step — pose, render, loss and backward — captured in
+    a CUDA graph and replayed: the step's ~100 small torch launches and the
+    Python autograd pass cost no host time per step, so the GPU runs the
+    render kernels back to back.
+
+    `loss_fn(image, target)` returns a scalar. The pose parameters of `reg`
+    (and the subject's volume, if it requires a gradient) are the graph's
+    static inputs: change them in place (`copy_`) between replays. After each
+    `replay()`, `loss` holds the step's loss and `grads` (the parameters'
+    `.grad` tensors at capture: pose rotation, translation, then the volume
+    when it requires a gradient) its gradients, overwritten by each replay.
+    Everything the render call does runs on the current stream without host
+    synchronisation or device allocation inside the C library, which is what
+    makes it capturable."""
+
+    def __init__(self, reg: Registration, loss_fn, target: torch.Tensor, n_samples: int = 500, warmup: int = 3):
+        self.reg = reg
+        self.loss_fn = loss_fn
+        self.target = target
+        self.n_samples = n_samples
+        self.params = [p for p in list(reg.parameters()) + [reg.subject._image_hu] if p.requires_grad]
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(warmup):
+                self._zero()
+                self._step()
+        torch.cuda.current_stream().wait_stream(side)
+        self._zero()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.loss = self._step()
+        # the graph's own gradient tensors (a later capture may rebind .grad)
+        self.grads = [p.grad for p in self.params]
+
+    def _zero(self):
+        for p in self.params:
+            p.grad = None
+
+    def _step(self) -> torch.Tensor:
+        img = self.reg(n_samples=self.n_samples)
+        loss = self.loss_fn(img, self.target)
+        loss.backward()
+        return loss.detach()
+
+    def replay(self) -> torch.Tensor:
+        self.graph.replay()
+        return self.loss
