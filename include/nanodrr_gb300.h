@@ -270,6 +270,27 @@ NDRR_API int32_t ndrr_raymarch_bwd_noalloc(const ndrr_raymarch_args* args, void*
  * in shared memory once per CTA. No counterpart in the reference. */
 NDRR_API int32_t ndrr_skip_windows(const ndrr_raymarch_args* args, int32_t* windows, void* stream);
 
+/* ---- intrinsics resample ---------------------------------------------------- *
+ * Replaces the reference's camera/homography.py:6-58 `resample`: each
+ * destination pixel (x, y) of image b samples the source image at
+ * hom_b (x, y, 1) (perspective divide), bilinearly with align_corners
+ * semantics and zero padding. img/out: [B, C, H, W] float32, contiguous;
+ * hom: [B, 3, 3] float32 = K_old K_new^-1 (the caller forms it from the two
+ * inverse intrinsics). */
+NDRR_API int32_t ndrr_homography_resample(const float* img, const float* hom, int32_t B, int32_t C, int32_t H,
+                                          int32_t W, float* out, void* stream);
+
+/* Scratch bytes of ndrr_homography_resample_bwd (per-CTA partials of the
+ * homography gradient). */
+NDRR_API int32_t ndrr_homography_resample_bwd_workspace_bytes(int32_t B, int32_t H, int32_t W, uint64_t* bytes);
+
+/* Adjoint of ndrr_homography_resample for the upstream gradient go: gimg
+ * ([B, C, H, W], ACCUMULATED into with atomics, zero it first; or NULL) and
+ * ghom ([B, 3, 3], written, deterministic fixed-order reduction; or NULL). */
+NDRR_API int32_t ndrr_homography_resample_bwd(const float* go, const float* img, const float* hom, int32_t B,
+                                              int32_t C, int32_t H, int32_t W, float* gimg, float* ghom,
+                                              void* workspace, uint64_t workspace_bytes, void* stream);
+
 /* ---- persistent batched launch -------------------------------------------- *
  * Many render requests — different volumes (same dtype), detector sizes and
  * sample counts — marched by ONE persistent kernel: CTAs take (request, tile)

@@ -9,11 +9,13 @@ hand-written CUDA kernels behind a C ABI (`include/nanodrr_gb300.h`).
 from ._build import build
 from .drr import DRR
 from .geometry import convert, make_k_inv, make_rt_inv, transform_point
+from .homography import resample
 from .raymarch import fused_raymarch, fused_raymarch_bwd, raymarch_backward, raymarch_forward
 from .renderer import fused_supported, render
 from .subject import Subject, hu_to_mu
 
 __all__ = [
+    "resample",
     "build",
     "DRR",
     "Subject",

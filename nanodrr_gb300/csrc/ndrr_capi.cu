@@ -219,6 +219,54 @@ int32_t ndrr_skip_windows(const ndrr_raymarch_args* a, int32_t* windows, void* s
     return ok();
 }
 
+static int32_t homography_check(const float* img, const float* hom, int32_t B, int32_t C, int32_t H, int32_t W) {
+    if (B < 0 || C < 1 || H < 2 || W < 2)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "resample needs B >= 0, C >= 1 and H, W >= 2 (got %d, %d, %d, %d)", B,
+                    C, H, W);
+    if ((long long)B * C * H * W >= kInt32Max * 4LL)
+        return fail(NDRR_ERR_LIMIT, "resample of %d x %d x %d x %d pixels is too large", B, C, H, W);
+    if (B > 65535) return fail(NDRR_ERR_LIMIT, "resample handles at most 65535 images per call (got %d)", B);
+    if (B > 0 && (img == nullptr || hom == nullptr))
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "img and hom must be non-NULL");
+    return NDRR_OK;
+}
+
+int32_t ndrr_homography_resample(const float* img, const float* hom, int32_t B, int32_t C, int32_t H, int32_t W,
+                                 float* out, void* stream) {
+    int32_t rc = homography_check(img, hom, B, C, H, W);
+    if (rc != NDRR_OK) return rc;
+    if (B == 0) return ok();
+    if (out == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "out is NULL");
+    const cudaError_t e = ndrr::launch_homography_fwd(img, hom, B, C, H, W, out, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "resample launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
+int32_t ndrr_homography_resample_bwd_workspace_bytes(int32_t B, int32_t H, int32_t W, uint64_t* bytes) {
+    if (bytes == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "bytes is NULL");
+    if (B < 0 || H < 2 || W < 2) return fail(NDRR_ERR_INVALID_ARGUMENT, "bad resample shape");
+    *bytes = (uint64_t)B * ndrr::homography_blocks(H, W) * 9 * sizeof(float);
+    return ok();
+}
+
+int32_t ndrr_homography_resample_bwd(const float* go, const float* img, const float* hom, int32_t B, int32_t C,
+                                     int32_t H, int32_t W, float* gimg, float* ghom, void* workspace,
+                                     uint64_t workspace_bytes, void* stream) {
+    int32_t rc = homography_check(img, hom, B, C, H, W);
+    if (rc != NDRR_OK) return rc;
+    if (B == 0) return ok();
+    if (go == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "go is NULL");
+    const uint64_t need = (uint64_t)B * ndrr::homography_blocks(H, W) * 9 * sizeof(float);
+    if (ghom != nullptr && (workspace == nullptr || workspace_bytes < need))
+        return fail(NDRR_ERR_WORKSPACE, "resample adjoint needs %llu workspace bytes, got %llu",
+                    (unsigned long long)need, (unsigned long long)(workspace ? workspace_bytes : 0));
+    const cudaError_t e = ndrr::launch_homography_bwd(go, img, hom, B, C, H, W, gimg, ghom,
+                                                      reinterpret_cast<float*>(workspace),
+                                                      reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "resample adjoint launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
 int32_t ndrr_quad_dims(int32_t D, int32_t H, int32_t W, int32_t* qz, int32_t* qy, int32_t* qx) {
     if (qz == nullptr || qy == nullptr || qx == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "NULL output");
     if (D < 1 || H < 1 || W < 1) return fail(NDRR_ERR_INVALID_ARGUMENT, "dims must be positive");

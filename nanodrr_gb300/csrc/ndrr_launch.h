@@ -30,6 +30,11 @@ cudaError_t launch_fwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaS
 cudaError_t launch_skip_windows(const ndrr_raymarch_args& a, int32_t* windows, cudaStream_t st);
 cudaError_t launch_bwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
 uint64_t slab_workspace_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
+int homography_blocks(int H, int W);
+cudaError_t launch_homography_fwd(const float* img, const float* hom, int B, int C, int H, int W, float* out,
+                                  cudaStream_t st);
+cudaError_t launch_homography_bwd(const float* go, const float* img, const float* hom, int B, int C, int H, int W,
+                                  float* gimg, float* ghom, float* partials, cudaStream_t st);
 cudaError_t launch_batched(const ndrr_batch_args& a, bool backward, int sm_count, cudaStream_t st);
 cudaError_t launch_occupancy(const void* vol, int vol_dtype, int D, int H, int W, int cell, int max_dist,
                              uint8_t* dist, uint8_t* scratch, cudaStream_t st);

@@ -23,9 +23,12 @@ the reference imports) — see tests/test_oracle.py.
 """
 
 from .grid_oracle import make_src, make_tgt, render_oracle, render_oracle_chunked, voxel_to_grid
+from .homography_oracle import resample_oracle, resample_pixels
 from .numpy_oracle import march_numpy, march_numpy_adjoint
 
 __all__ = [
+    "resample_oracle",
+    "resample_pixels",
     "make_src",
     "make_tgt",
     "render_oracle",

@@ -29,8 +29,8 @@ def subject_from_arrays(vol, lab, voxel_to_world, C, dtype=torch.float32, device
 
 
 def rel_maxabs(out, ref) -> float:
-    out = torch.as_tensor(out).double().cpu()
-    ref = torch.as_tensor(ref).double().cpu()
+    out = torch.as_tensor(out).detach().double().cpu()
+    ref = torch.as_tensor(ref).detach().double().cpu()
     return float((out - ref).abs().max() / ref.abs().max().clamp_min(1e-30))
 
 

@@ -15,9 +15,12 @@ Cases mirror the reference's own tests:
                   (persp/ortho × C=1/3), pose, volume and intrinsics
                   gradients (:68-144), pose-batch broadcast (:192-209), in
                   float32 and float64;
-  phantom40.npz — a 40³ version of the seeded CT phantom, C=1 and C=8.
+  phantom40.npz — a 40³ version of the seeded CT phantom, C=1 and C=8;
+  homography.npz — the reference's 2-D intrinsics resample
+                  (src/nanodrr/camera/homography.py:6-58) in float64: output
+                  and gradients to the image and both inverse intrinsics.
 
-Usage: python tests/golden/make_golden.py [/path/to/reference]
+Usage: python tests/golden/make_golden.py [/path/to/reference] [case ...]
 """
 
 from __future__ import annotations
@@ -198,8 +201,30 @@ def phantom40():
     print("phantom40 done")
 
 
+def homography():
+    from nanodrr.camera.homography import resample as ref_resample
+
+    g = torch.Generator().manual_seed(11)
+    B, C, H, W = 2, 3, 17, 23
+    img = torch.rand(B, C, H, W, generator=g, dtype=torch.float64)
+    k_old = torch.stack([make_k_inv(1020.0, 1.4, 1.5, 2.0, -3.0, H, W, dtype=torch.float64)[0],
+                         make_k_inv(1000.0, 1.3, 1.3, -1.0, 1.0, H, W, dtype=torch.float64)[0]])
+    k_new = torch.stack([make_k_inv(1060.0, 1.2, 1.4, -2.0, 2.5, H, W, dtype=torch.float64)[0],
+                         make_k_inv(990.0, 1.35, 1.25, 0.5, -0.5, H, W, dtype=torch.float64)[0]])
+    go = torch.randn(B, C, H, W, generator=g, dtype=torch.float64)
+    img_r, ko_r, kn_r = (x.clone().requires_grad_(True) for x in (img, k_old, k_new))
+    out = ref_resample(img_r, ko_r, kn_r)
+    (out * go).sum().backward()
+    np.savez_compressed(
+        HERE / "homography.npz", img=img.numpy(), k_inv_old=k_old.numpy(), k_inv_new=k_new.numpy(),
+        go=go.numpy(), out=out.detach().numpy(), g_img=img_r.grad.numpy(), g_k_inv_old=ko_r.grad.numpy(),
+        g_k_inv_new=kn_r.grad.numpy(),
+    )
+    print("homography done")
+
+
 if __name__ == "__main__":
     torch.set_num_threads(min(8, os.cpu_count() or 1))
-    impulse()
-    random32()
-    phantom40()
+    cases = {"impulse": impulse, "random32": random32, "phantom40": phantom40, "homography": homography}
+    for name in (sys.argv[2:] or list(cases)):
+        cases[name]()

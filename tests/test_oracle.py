@@ -153,3 +153,20 @@ def test_numpy_adjoint_camera_terms_central_differences():
     e[3, 3, 4] = 1.0
     fv = lambda v: float((march_numpy(v, None, M, src, tgt, step, n) * go).sum())  # noqa: E731
     assert abs((fv(vol + e) - fv(vol - e)) / 2 - gvol[3, 3, 4]) < 1e-9
+
+
+def test_homography_oracle_matches_reference_golden():
+    from pathlib import Path
+
+    from oracle import resample_oracle, resample_pixels
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "homography.npz")
+    img, ko, kn = (torch.from_numpy(g[k]).requires_grad_(True) for k in ("img", "k_inv_old", "k_inv_new"))
+    out = resample_oracle(img, ko, kn)
+    assert _rel(out.detach(), g["out"]) < 1e-12
+    (out * torch.from_numpy(g["go"])).sum().backward()
+    for name, t in (("g_img", img), ("g_k_inv_old", ko), ("g_k_inv_new", kn)):
+        assert _rel(t.grad, g[name]) < 1e-10, name
+    # the per-corner form the kernel follows
+    Hm = torch.linalg.inv(ko.detach()) @ kn.detach()
+    assert _rel(resample_pixels(img.detach(), Hm), g["out"]) < 1e-9
