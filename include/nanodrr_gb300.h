@@ -291,6 +291,27 @@ NDRR_API int32_t ndrr_homography_resample_bwd(const float* go, const float* img,
                                               int32_t C, int32_t H, int32_t W, float* gimg, float* ghom,
                                               void* workspace, uint64_t workspace_bytes, void* stream);
 
+/* ---- normalised cross-correlation ------------------------------------------ *
+ * Replaces the reference's metrics/ncc.py:8-37 NormalizedCrossCorrelation2d
+ * (the image-similarity loss of a registration step). x1, x2: [B, P, N]
+ * float32, contiguous: B batch elements of P planes of N pixels (P = C image
+ * channels, or C x patches when the caller unfolds local windows into
+ * planes). Each plane of each image is centred and divided by
+ * sqrt(population variance + eps); score[b] = sum over its planes and pixels
+ * of the products / (P N). stats: [B, P, NDRR_NCC_STATS] float32, written
+ * by the forward and read by the adjoint; workspace: the forward's per-chunk
+ * moments (ndrr_ncc_workspace_bytes). */
+#define NDRR_NCC_STATS 8
+NDRR_API int32_t ndrr_ncc_workspace_bytes(int32_t B, int32_t P, int32_t N, uint64_t* bytes);
+NDRR_API int32_t ndrr_ncc_fwd(const float* x1, const float* x2, int32_t B, int32_t P, int32_t N, float eps,
+                              float* score, float* stats, void* workspace, uint64_t workspace_bytes,
+                              void* stream);
+
+/* Adjoint for the upstream gradient go [B]: g1 = d/dx1, g2 = d/dx2 ([B, P, N],
+ * written; either may be NULL). */
+NDRR_API int32_t ndrr_ncc_bwd(const float* go, const float* x1, const float* x2, const float* stats, int32_t B,
+                              int32_t P, int32_t N, float* g1, float* g2, void* stream);
+
 /* ---- persistent batched launch -------------------------------------------- *
  * Many render requests — different volumes (same dtype), detector sizes and
  * sample counts — marched by ONE persistent kernel: CTAs take (request, tile)
@@ -387,8 +408,8 @@ NDRR_API int32_t ndrr_occupancy_build(const ndrr_occupancy_args* args, void* str
  * interval starts and ends. fp32 master parameters (NDRR_PROPOSAL_PARAMS
  * floats: W1 [64][64], b1, W2 [64][64], b2, W3 [2][64], b3) are trained by the
  * kernels below and packed to bf16 (NDRR_PROPOSAL_PACKED_BYTES) for the
- * tensor-core inference inside the render kernels. No counterpart in the
- * reference. */
+ * tensor-core inference in the window kernel (ndrr_skip_windows). No
+ * counterpart in the reference. */
 #define NDRR_PROPOSAL_PARAMS 8450
 #define NDRR_PROPOSAL_PACKED_BYTES 17952
 #define NDRR_PROPOSAL_FEATURES 64

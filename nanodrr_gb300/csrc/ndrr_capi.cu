@@ -267,6 +267,54 @@ int32_t ndrr_homography_resample_bwd(const float* go, const float* img, const fl
     return ok();
 }
 
+static int32_t ncc_check(const float* x1, const float* x2, int32_t B, int32_t P, int32_t N, const float* stats) {
+    if (B < 0 || P < 1 || N < 1)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "ncc needs B >= 0, P >= 1, N >= 1 (got %d, %d, %d)", B, P, N);
+    if ((long long)B * P >= kInt32Max || (long long)B * P * N >= kInt32Max * 16LL)
+        return fail(NDRR_ERR_LIMIT, "ncc of %d x %d planes of %d pixels is too large", B, P, N);
+    if (B > 0 && (x1 == nullptr || x2 == nullptr || stats == nullptr))
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "x1, x2 and stats must be non-NULL");
+    return NDRR_OK;
+}
+
+int32_t ndrr_ncc_workspace_bytes(int32_t B, int32_t P, int32_t N, uint64_t* bytes) {
+    if (bytes == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "bytes is NULL");
+    if (B < 0 || P < 1 || N < 1) return fail(NDRR_ERR_INVALID_ARGUMENT, "bad ncc shape");
+    *bytes = ndrr::ncc_workspace_bytes(B, P, N);
+    return ok();
+}
+
+int32_t ndrr_ncc_fwd(const float* x1, const float* x2, int32_t B, int32_t P, int32_t N, float eps, float* score,
+                     float* stats, void* workspace, uint64_t workspace_bytes, void* stream) {
+    int32_t rc = ncc_check(x1, x2, B, P, N, stats);
+    if (rc != NDRR_OK) return rc;
+    if (!(eps >= 0.f)) return fail(NDRR_ERR_INVALID_ARGUMENT, "eps must be >= 0");
+    if (B == 0) return ok();
+    if (score == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "score is NULL");
+    if ((long long)N > 65535LL * 4096) return fail(NDRR_ERR_LIMIT, "ncc planes hold at most 268 M pixels");
+    const uint64_t need = ndrr::ncc_workspace_bytes(B, P, N);
+    if (workspace == nullptr || workspace_bytes < need)
+        return fail(NDRR_ERR_WORKSPACE, "ncc needs %llu workspace bytes, got %llu", (unsigned long long)need,
+                    (unsigned long long)(workspace ? workspace_bytes : 0));
+    const cudaError_t e = ndrr::launch_ncc_fwd(x1, x2, B, P, N, eps, score, stats, workspace,
+                                               reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "ncc launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
+int32_t ndrr_ncc_bwd(const float* go, const float* x1, const float* x2, const float* stats, int32_t B, int32_t P,
+                     int32_t N, float* g1, float* g2, void* stream) {
+    int32_t rc = ncc_check(x1, x2, B, P, N, stats);
+    if (rc != NDRR_OK) return rc;
+    if (B == 0 || (g1 == nullptr && g2 == nullptr)) return ok();
+    if (go == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "go is NULL");
+    if ((long long)N > 65535LL * 4096) return fail(NDRR_ERR_LIMIT, "ncc planes hold at most 268 M pixels");
+    const cudaError_t e =
+        ndrr::launch_ncc_bwd(go, x1, x2, stats, B, P, N, g1, g2, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "ncc adjoint launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
 int32_t ndrr_quad_dims(int32_t D, int32_t H, int32_t W, int32_t* qz, int32_t* qy, int32_t* qx) {
     if (qz == nullptr || qy == nullptr || qx == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "NULL output");
     if (D < 1 || H < 1 || W < 1) return fail(NDRR_ERR_INVALID_ARGUMENT, "dims must be positive");

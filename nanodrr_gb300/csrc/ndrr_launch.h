@@ -31,6 +31,11 @@ cudaError_t launch_skip_windows(const ndrr_raymarch_args& a, int32_t* windows, c
 cudaError_t launch_bwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
 uint64_t slab_workspace_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
 int homography_blocks(int H, int W);
+size_t ncc_workspace_bytes(int B, int P, int N);
+cudaError_t launch_ncc_fwd(const float* x1, const float* x2, int B, int P, int N, float eps, float* score,
+                           float* stats, void* workspace, cudaStream_t st);
+cudaError_t launch_ncc_bwd(const float* go, const float* x1, const float* x2, const float* stats, int B, int P,
+                           int N, float* g1, float* g2, cudaStream_t st);
 cudaError_t launch_homography_fwd(const float* img, const float* hom, int B, int C, int H, int W, float* out,
                                   cudaStream_t st);
 cudaError_t launch_homography_bwd(const float* go, const float* img, const float* hom, int B, int C, int H, int W,

@@ -1,13 +1,14 @@
 // Empty-space sample windows computed ahead of the march (ndrr_skip_windows).
 //
-// The fused proposal kernels run the network inside the render kernel; its
-// weights (19.7 KB of shared memory per CTA) and fragment registers lower the
-// occupancy of the whole march. Here the network and the occupancy check run
-// once per ray in their own persistent kernel and leave each ray's sample
-// window [lo, hi) in a [B, N, 2] int32 buffer (8 bytes per ray), which the
-// plain march kernels read in their ray set-up; the forward and the adjoint
-// of one step share it. Windows are the ones apply_skip computes in-kernel,
-// so both routes give identical samples.
+// Running the network inside the render kernels would cost the whole march
+// occupancy (19.7 KB of shared memory for the weights per CTA, and the
+// fragment registers); measured that way the learned forward took 6.0 ms
+// against 0.7 + 1.8 ms here. So the network and the occupancy check run once
+// per ray in their own persistent kernel and leave each ray's sample window
+// [lo, hi) in a [B, N, 2] int32 buffer (8 bytes per ray), which the plain
+// march kernels read in their ray set-up; the forward and the adjoint of one
+// step share it. The occupancy skip computes the same windows (apply_skip)
+// either here or inside the march.
 #include "ndrr_march.cuh"
 
 namespace ndrr {

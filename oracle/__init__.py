@@ -24,9 +24,11 @@ the reference imports) — see tests/test_oracle.py.
 
 from .grid_oracle import make_src, make_tgt, render_oracle, render_oracle_chunked, voxel_to_grid
 from .homography_oracle import resample_oracle, resample_pixels
+from .ncc_oracle import ncc_oracle
 from .numpy_oracle import march_numpy, march_numpy_adjoint
 
 __all__ = [
+    "ncc_oracle",
     "resample_oracle",
     "resample_pixels",
     "make_src",

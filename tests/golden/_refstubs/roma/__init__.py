@@ -7,4 +7,4 @@ def _unavailable(*a, **k):
 
 
 euler_to_rotmat = rotmat_to_euler = unitquat_to_rotmat = quat_wxyz_to_xyzw = _unavailable
-special_procrustes = rotvec_to_rotmat = rotmat_to_rotvec = _unavailable
+special_procrustes = rotvec_to_rotmat = rotmat_to_rotvec = rotmat_geodesic_distance = _unavailable

@@ -18,7 +18,10 @@ Cases mirror the reference's own tests:
   phantom40.npz — a 40³ version of the seeded CT phantom, C=1 and C=8;
   homography.npz — the reference's 2-D intrinsics resample
                   (src/nanodrr/camera/homography.py:6-58) in float64: output
-                  and gradients to the image and both inverse intrinsics.
+                  and gradients to the image and both inverse intrinsics;
+  ncc.npz       — the reference's NormalizedCrossCorrelation2d
+                  (src/nanodrr/metrics/ncc.py) in float64, global and 5x5
+                  patches: scores and gradients to both images.
 
 Usage: python tests/golden/make_golden.py [/path/to/reference] [case ...]
 """
@@ -223,8 +226,29 @@ def homography():
     print("homography done")
 
 
+def ncc():
+    from nanodrr.metrics.ncc import NormalizedCrossCorrelation2d as RefNCC
+
+    g = torch.Generator().manual_seed(12)
+    B, C, H, W = 3, 2, 20, 24
+    x1 = torch.rand(B, C, H, W, generator=g, dtype=torch.float64)
+    x2 = 0.6 * x1 + 0.4 * torch.rand(B, C, H, W, generator=g, dtype=torch.float64)
+    go = torch.randn(B, generator=g, dtype=torch.float64)
+    res = {"x1": x1.numpy(), "x2": x2.numpy(), "go": go.numpy()}
+    for tag, patch in (("global", None), ("patch5", 5)):
+        a, b = x1.clone().requires_grad_(True), x2.clone().requires_grad_(True)
+        s = RefNCC(patch_size=patch)(a, b)
+        (s * go).sum().backward()
+        res[f"score_{tag}"] = s.detach().numpy()
+        res[f"g1_{tag}"] = a.grad.numpy()
+        res[f"g2_{tag}"] = b.grad.numpy()
+    np.savez_compressed(HERE / "ncc.npz", **res)
+    print("ncc done")
+
+
 if __name__ == "__main__":
     torch.set_num_threads(min(8, os.cpu_count() or 1))
-    cases = {"impulse": impulse, "random32": random32, "phantom40": phantom40, "homography": homography}
+    cases = {"impulse": impulse, "random32": random32, "phantom40": phantom40, "homography": homography,
+             "ncc": ncc}
     for name in (sys.argv[2:] or list(cases)):
         cases[name]()

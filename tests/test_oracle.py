@@ -170,3 +170,18 @@ def test_homography_oracle_matches_reference_golden():
     # the per-corner form the kernel follows
     Hm = torch.linalg.inv(ko.detach()) @ kn.detach()
     assert _rel(resample_pixels(img.detach(), Hm), g["out"]) < 1e-9
+
+
+@pytest.mark.parametrize("tag,patch", [("global", None), ("patch5", 5)])
+def test_ncc_oracle_matches_reference_golden(tag, patch):
+    from pathlib import Path
+
+    from oracle import ncc_oracle
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "ncc.npz")
+    x1, x2 = (torch.from_numpy(g[k]).requires_grad_(True) for k in ("x1", "x2"))
+    s = ncc_oracle(x1, x2, patch)
+    assert _rel(s.detach(), g[f"score_{tag}"]) < 1e-12
+    (s * torch.from_numpy(g["go"])).sum().backward()
+    assert _rel(x1.grad, g[f"g1_{tag}"]) < 1e-10
+    assert _rel(x2.grad, g[f"g2_{tag}"]) < 1e-10

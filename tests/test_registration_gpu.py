@@ -14,7 +14,7 @@ from nanodrr_gb300 import phantom
 from nanodrr_gb300.geometry import convert
 from nanodrr_gb300.registration import NormalizedCrossCorrelation2d, Registration
 from nanodrr_gb300.renderer import _make_src, _make_tgt
-from oracle import render_oracle
+from oracle import ncc_oracle, render_oracle
 
 pytestmark = pytest.mark.gpu
 DEV = "cuda"
@@ -66,7 +66,7 @@ def test_registration_pose_gradient_matches_central_differences():
         T = convert(params[:, :3], params[:, 3:], "so3_log")
         pose = rt64 @ piv @ T @ piv_inv
         img = render_oracle(vol64, None, w2v, pose, src, tgt, n).reshape(B, 1, det, det)
-        return -ncc(img, target64).sum()
+        return -ncc_oracle(img, target64).sum()
 
     h = 1e-3
     fd = torch.zeros(B, 6, dtype=torch.float64)
