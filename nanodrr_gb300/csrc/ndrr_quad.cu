@@ -50,18 +50,42 @@ __global__ void quad_build_b16_kernel(const uint16_t* __restrict__ v, int D, int
 
 // gvol[z][y][x] += the four quad entries in which voxel (x, y) of plane z is
 // a corner: (x, y) as (x0, y0), (x0 + 1, y0), (x0, y0 + 1), (x0 + 1, y0 + 1).
-__global__ void quad_fold_kernel(const float4* __restrict__ gq, int D, int H, int W, float* __restrict__ gvol) {
+// One CTA per (z, y) line of the volume, four consecutive x per thread: the
+// five quad entries of each of the two quad rows a thread needs are 16-byte
+// loads, and no 64-bit index division is needed.
+__global__ void __launch_bounds__(128) quad_fold_kernel(const float4* __restrict__ gq, int D, int H, int W,
+                                                        float* __restrict__ gvol) {
     const int QX = W + 3, QY = H + 3;
-    const long long n = (long long)D * H * W;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const int x = (int)(i % W), y = (int)((i / W) % H), z = (int)(i / ((long long)W * H));
-        const size_t row = ((size_t)(z + 2) * QY + (y + 2)) * QX;
-        const size_t rowm = row - QX;  // y0 = y - 1
-        const float a = __ldg(&gq[row + x + 2].x);
-        const float b = __ldg(&gq[row + x + 1].y);
-        const float c = __ldg(&gq[rowm + x + 2].z);
-        const float d = __ldg(&gq[rowm + x + 1].w);
-        gvol[i] += (a + b) + (c + d);
+    const int line = blockIdx.x;  // z * H + y
+    const int z = line / H, y = line - z * H;
+    const float4* __restrict__ r0 = gq + ((size_t)(z + 2) * QY + (y + 2)) * QX;  // entries with y0 = y
+    const float4* __restrict__ r1 = r0 - QX;                                      // entries with y0 = y - 1
+    float* __restrict__ out = gvol + (size_t)line * W;
+    const bool vec = (W & 3) == 0;
+    for (int x0 = threadIdx.x * 4; x0 < W; x0 += blockDim.x * 4) {
+        // entries x0 + 1 .. x0 + 5 (all inside the padded row of W + 3)
+        float4 a[5], c[5];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const int e = min(x0 + 1 + k, QX - 1);
+            a[k] = __ldg(r0 + e);
+            c[k] = __ldg(r1 + e);
+        }
+        float v[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = (a[j + 1].x + a[j].y) + (c[j + 1].z + c[j].w);
+        if (vec) {
+            float4 o = *reinterpret_cast<float4*>(out + x0);
+            o.x += v[0];
+            o.y += v[1];
+            o.z += v[2];
+            o.w += v[3];
+            *reinterpret_cast<float4*>(out + x0) = o;
+        } else {
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (x0 + j < W) out[x0 + j] += v[j];
+        }
     }
 }
 
@@ -79,8 +103,7 @@ cudaError_t launch_quad_build(const void* vol, int dtype, int D, int H, int W, v
 }
 
 cudaError_t launch_quad_fold(const float* gquad, int D, int H, int W, float* gvol, cudaStream_t st) {
-    const long long n = (long long)D * H * W;
-    quad_fold_kernel<<<grid_for(n), 256, 0, st>>>((const float4*)gquad, D, H, W, gvol);
+    quad_fold_kernel<<<(unsigned)((long long)D * H), 128, 0, st>>>((const float4*)gquad, D, H, W, gvol);
     return cudaGetLastError();
 }
 
