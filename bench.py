@@ -411,6 +411,20 @@ def run_ours(args, world, rank, local):
         "plain_layout_bwd_ms": round(statistics.median(times["bwd_plain_layout"]), 3),
         "direct_scatter_bwd_ms": round(statistics.median(times["bwd_direct"]), 3),
     }
+    # ---- texture-filtered forward variant (8-bit hardware weights)
+    from nanodrr_gb300.raymarch import TextureVolume
+
+    with torch.no_grad():
+        tex = TextureVolume(vol)
+        soft, _ = raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd)
+        hard, _ = raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, texture=tex)
+        texture_variant = {
+            "fwd_ms": round(_event_ms(lambda: raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, texture=tex),
+                                      max(3, args.steps)), 3),
+            "rel_maxabs_vs_software": round(_rel_maxabs(hard, soft), 6),
+        }
+        tex.close()
+        del soft, hard
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, sub, k_inv, sdd, rt)
@@ -449,6 +463,7 @@ def run_ours(args, world, rank, local):
         },
         "methods_frames_per_s": table,
         "methods_frames_per_s_eager": eager,
+        "texture_variant": texture_variant,
         "learned_vs_plain": round(table["learned"] / table["plain"], 3),
         "learned_vs_plain_pose_only": round(table["learned_pose_only"] / table["plain_pose_only"], 3),
         "proposal": {

@@ -185,7 +185,12 @@ typedef struct ndrr_raymarch_args {
                                at most 57344)                                   */
     int32_t slab_mib;       /* gvol_mode 3 (and auto): quad-gradient MiB per
                                slab (0 default = 96, at most 4096)              */
-    int32_t reserved[2];
+    /* Texture-filtered forward (a measured variant, not the default): a
+     * handle from ndrr_texture_create. When set, ndrr_raymarch_fwd samples
+     * it with the texture unit's trilinear filter, whose interpolation
+     * weights have 8 fractional bits (results differ from the fp32 path by
+     * about 1e-3 relative); one channel, no skipping, no quad layout. */
+    uint64_t vol_texture;
 } ndrr_raymarch_args;
 
 enum ndrr_skip_mode {
@@ -269,6 +274,14 @@ NDRR_API int32_t ndrr_raymarch_bwd_noalloc(const ndrr_raymarch_args* args, void*
  * operands, fp32 accumulation) in a persistent kernel that stages its weights
  * in shared memory once per CTA. No counterpart in the reference. */
 NDRR_API int32_t ndrr_skip_windows(const ndrr_raymarch_args* args, int32_t* windows, void* stream);
+
+/* 3-D texture of a float32 volume [D, H, W] for the texture-filtered forward
+ * variant: allocates a CUDA array (D x H x W floats), copies the volume on
+ * `stream`, and creates a texture object with linear filtering and zero
+ * border; *handle receives it. ndrr_texture_destroy frees both. */
+NDRR_API int32_t ndrr_texture_create(const float* vol, int32_t D, int32_t H, int32_t W, uint64_t* handle,
+                                     void* stream);
+NDRR_API int32_t ndrr_texture_destroy(uint64_t handle);
 
 /* ---- intrinsics resample ---------------------------------------------------- *
  * Replaces the reference's camera/homography.py:6-58 `resample`: each

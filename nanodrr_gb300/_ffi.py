@@ -90,7 +90,7 @@ class RaymarchArgs(ctypes.Structure):
         ("gvol_mode", ctypes.c_int32),
         ("brick_cap", ctypes.c_int32),
         ("slab_mib", ctypes.c_int32),
-        ("reserved", ctypes.c_int32 * 2),
+        ("vol_texture", ctypes.c_uint64),
     ]
 
     def __init__(self, **kw):
@@ -148,6 +148,9 @@ SIGNATURES: dict[str, tuple] = {
     "ndrr_occupancy_dims": (ctypes.c_int32, [ctypes.c_int32] * 4 + [_i32p] * 3),
     "ndrr_occupancy_build": (ctypes.c_int32, [ctypes.POINTER(OccupancyArgs), ctypes.c_void_p]),
     "ndrr_skip_windows": (ctypes.c_int32, [ctypes.POINTER(RaymarchArgs), ctypes.c_void_p, ctypes.c_void_p]),
+    "ndrr_texture_create": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                             ctypes.POINTER(ctypes.c_uint64), ctypes.c_void_p]),
+    "ndrr_texture_destroy": (ctypes.c_int32, [ctypes.c_uint64]),
     "ndrr_ncc_workspace_bytes": (ctypes.c_int32, [ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                                                   ctypes.POINTER(ctypes.c_uint64)]),
     "ndrr_ncc_fwd": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,

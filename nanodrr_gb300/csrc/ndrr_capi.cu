@@ -155,6 +155,18 @@ int32_t ndrr_raymarch_fwd(const ndrr_raymarch_args* a, void* stream) {
     if (a->vol_quad != nullptr && a->out_dtype != a->vol_dtype)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "the quad layout writes the output in the volume's dtype");
     const ndrr::LaunchShape ls = ndrr::choose_shape(*a, sm_count_current());
+    if (a->vol_texture != 0) {
+        if (a->n_classes != 1 || a->skip_mode != NDRR_SKIP_NONE || a->vol_quad != nullptr ||
+            a->sample_window != nullptr || a->out_total != nullptr || a->out_extent != nullptr)
+            return fail(NDRR_ERR_INVALID_ARGUMENT,
+                        "the texture-filtered forward takes one channel, no skipping, windows, quad layout, total or "
+                        "extent output");
+        rc = validate_shape(ls, (size_t)ls.tw * ls.th * ls.K * sizeof(float));
+        if (rc != NDRR_OK) return rc;
+        const cudaError_t e = ndrr::launch_fwd_tex(*a, ls, reinterpret_cast<cudaStream_t>(stream));
+        if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "texture forward launch failed: %s", cudaGetErrorString(e));
+        return ok();
+    }
     rc = validate_shape(ls, ndrr::fwd_smem_bytes(*a, ls));
     if (rc != NDRR_OK) return rc;
     const cudaError_t e = ndrr::launch_fwd(*a, ls, reinterpret_cast<cudaStream_t>(stream));
@@ -312,6 +324,25 @@ int32_t ndrr_ncc_bwd(const float* go, const float* x1, const float* x2, const fl
     const cudaError_t e =
         ndrr::launch_ncc_bwd(go, x1, x2, stats, B, P, N, g1, g2, reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "ncc adjoint launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
+int32_t ndrr_texture_create(const float* vol, int32_t D, int32_t H, int32_t W, uint64_t* handle, void* stream) {
+    if (vol == nullptr || handle == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "vol and handle must be non-NULL");
+    if (D < 1 || H < 1 || W < 1 || D > 16384 || H > 16384 || W > 16384)
+        return fail(NDRR_ERR_LIMIT, "3-D texture extent %d x %d x %d outside [1, 16384]", D, H, W);
+    unsigned long long h = 0;
+    const cudaError_t e = ndrr::texture_create(vol, D, H, W, &h, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "texture creation failed: %s", cudaGetErrorString(e));
+    *handle = h;
+    return ok();
+}
+
+int32_t ndrr_texture_destroy(uint64_t handle) {
+    bool known = false;
+    const cudaError_t e = ndrr::texture_destroy(handle, &known);
+    if (!known) return fail(NDRR_ERR_INVALID_ARGUMENT, "unknown texture handle");
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "texture destruction failed: %s", cudaGetErrorString(e));
     return ok();
 }
 

@@ -441,3 +441,23 @@ def test_slab_mode_needs_the_quad_layout():
     go = torch.randn(1, 1, 64, device=DEV)
     with pytest.raises(ValueError, match="quad layout"):
         raymarch_backward(go, t(vol), t(vol), t(M), t(src), t(tgt), t(step), 100, 1, width, True, False, gvol_mode=3)
+
+
+def test_texture_filtered_forward_variant_is_close():
+    """The texture unit's trilinear filter (8-bit weights) against the fp32
+    software path: close (about 1e-3 relative), not equal."""
+    from nanodrr_gb300.raymarch import TextureVolume
+
+    n = 220
+    vol, lab, M, src, tgt, step, width = _random_case(51, B=2, Hd=24, Wd=20)
+    t = lambda a: torch.from_numpy(a).to(DEV)  # noqa: E731
+    v = t(vol)
+    tex = TextureVolume(v)
+    soft, _ = raymarch_forward(v, v, t(M), t(src), t(tgt), t(step), n, 1, width)
+    hard, _ = raymarch_forward(v, v, t(M), t(src), t(tgt), t(step), n, 1, width, texture=tex)
+    err = rel_maxabs(hard, soft)
+    assert err < 1e-2, err
+    assert float(hard.abs().max()) > 0
+    tex.close()
+    with pytest.raises(ValueError):
+        raymarch_forward(v, v, t(M), t(src), t(tgt), t(step), n, 1, width, texture=tex)
