@@ -424,7 +424,14 @@ def run_ours(args, world, rank, local):
             "rel_maxabs_vs_software": round(_rel_maxabs(hard, soft), 6),
         }
         tex.close()
-        del soft, hard
+        tma, _ = raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, fwd_mode=1)
+        plain16, _ = raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, tile=(16, 8, 1))
+        tma_variant = {
+            "fwd_ms": round(_event_ms(lambda: raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, fwd_mode=1),
+                                      max(3, args.steps)), 3),
+            "bitwise_equal_to_software": bool(torch.equal(tma, plain16)),
+        }
+        del soft, hard, tma, plain16
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, sub, k_inv, sdd, rt)
@@ -464,6 +471,7 @@ def run_ours(args, world, rank, local):
         "methods_frames_per_s": table,
         "methods_frames_per_s_eager": eager,
         "texture_variant": texture_variant,
+        "tma_staged_variant": tma_variant,
         "learned_vs_plain": round(table["learned"] / table["plain"], 3),
         "learned_vs_plain_pose_only": round(table["learned_pose_only"] / table["plain_pose_only"], 3),
         "proposal": {

@@ -185,6 +185,8 @@ typedef struct ndrr_raymarch_args {
                                at most 57344)                                   */
     int32_t slab_mib;       /* gvol_mode 3 (and auto): quad-gradient MiB per
                                slab (0 default = 96, at most 4096)              */
+    int32_t fwd_mode;       /* NDRR_FWD_* (0 default)                          */
+    int32_t pad0;
     /* Texture-filtered forward (a measured variant, not the default): a
      * handle from ndrr_texture_create. When set, ndrr_raymarch_fwd samples
      * it with the texture unit's trilinear filter, whose interpolation
@@ -192,6 +194,16 @@ typedef struct ndrr_raymarch_args {
      * about 1e-3 relative); one channel, no skipping, no quad layout. */
     uint64_t vol_texture;
 } ndrr_raymarch_args;
+
+/* Forward variants (ndrr_raymarch_args.fwd_mode). */
+enum ndrr_fwd_mode {
+    NDRR_FWD_DEFAULT = 0,  /* software trilinear from the volume or quad layout */
+    NDRR_FWD_TMA = 1,      /* measured variant: per-tile volume boxes staged into
+                              shared memory by 3-D TMA loads (f32 volume with W a
+                              multiple of 4, one channel, f32 output, no skipping,
+                              windows or quad layout); bitwise the default's
+                              image */
+};
 
 enum ndrr_skip_mode {
     NDRR_SKIP_NONE = 0,

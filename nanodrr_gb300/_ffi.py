@@ -90,6 +90,8 @@ class RaymarchArgs(ctypes.Structure):
         ("gvol_mode", ctypes.c_int32),
         ("brick_cap", ctypes.c_int32),
         ("slab_mib", ctypes.c_int32),
+        ("fwd_mode", ctypes.c_int32),
+        ("pad0", ctypes.c_int32),
         ("vol_texture", ctypes.c_uint64),
     ]
 

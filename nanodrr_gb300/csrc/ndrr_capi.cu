@@ -101,6 +101,8 @@ int32_t validate_common(const ndrr_raymarch_args* a) {
         return fail(NDRR_ERR_INVALID_ARGUMENT, "sample_window and skip_mode are exclusive (one skip at a time)");
     if (a->vol_quad != nullptr && (long long)(a->D + 4) * (a->H + 3) * (a->W + 3) >= kInt32Max)
         return fail(NDRR_ERR_LIMIT, "quad layout of a %dx%dx%d volume exceeds int32 indexing", a->D, a->H, a->W);
+    if (a->fwd_mode != NDRR_FWD_DEFAULT && a->fwd_mode != NDRR_FWD_TMA)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "fwd_mode must be 0 or 1 (got %d)", a->fwd_mode);
     if (a->gvol_mode < NDRR_GVOL_AUTO || a->gvol_mode > NDRR_GVOL_SLAB)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode must be 0, 1, 2 or 3 (got %d)", a->gvol_mode);
     if (a->gvol_mode == NDRR_GVOL_SLAB && a->vol_quad == nullptr)
@@ -155,6 +157,19 @@ int32_t ndrr_raymarch_fwd(const ndrr_raymarch_args* a, void* stream) {
     if (a->vol_quad != nullptr && a->out_dtype != a->vol_dtype)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "the quad layout writes the output in the volume's dtype");
     const ndrr::LaunchShape ls = ndrr::choose_shape(*a, sm_count_current());
+    if (a->fwd_mode == NDRR_FWD_TMA) {
+        if (a->vol_dtype != NDRR_F32 || a->out_dtype != NDRR_F32 || a->W % 4 != 0 || a->n_classes != 1 ||
+            a->skip_mode != NDRR_SKIP_NONE || a->vol_quad != nullptr || a->sample_window != nullptr ||
+            a->out_total != nullptr || a->out_extent != nullptr || a->vol_texture != 0)
+            return fail(NDRR_ERR_INVALID_ARGUMENT,
+                        "the TMA forward takes an f32 volume with W a multiple of 4, f32 output, one channel, "
+                        "no skipping, windows, quad layout, texture, total or extent output");
+        if (reinterpret_cast<uintptr_t>(a->vol) % 16 != 0)
+            return fail(NDRR_ERR_INVALID_ARGUMENT, "the TMA forward needs a 16-byte aligned volume");
+        const cudaError_t e = ndrr::launch_fwd_tma(*a, ls, reinterpret_cast<cudaStream_t>(stream));
+        if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "TMA forward launch failed: %s", cudaGetErrorString(e));
+        return ok();
+    }
     if (a->vol_texture != 0) {
         if (a->n_classes != 1 || a->skip_mode != NDRR_SKIP_NONE || a->vol_quad != nullptr ||
             a->sample_window != nullptr || a->out_total != nullptr || a->out_extent != nullptr)

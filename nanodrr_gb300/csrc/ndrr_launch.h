@@ -29,6 +29,7 @@ size_t brick_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
 cudaError_t launch_fwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
 cudaError_t launch_skip_windows(const ndrr_raymarch_args& a, int32_t* windows, cudaStream_t st);
 cudaError_t launch_fwd_tex(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
+cudaError_t launch_fwd_tma(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
 cudaError_t texture_create(const float* vol, int D, int H, int W, unsigned long long* handle, cudaStream_t st);
 cudaError_t texture_destroy(unsigned long long handle, bool* known);
 cudaError_t launch_bwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);

@@ -245,6 +245,7 @@ def raymarch_forward(
     quad: torch.Tensor | None = None,
     windows: torch.Tensor | None = None,
     texture: TextureVolume | None = None,
+    fwd_mode: int = 0,
 ) -> tuple[torch.Tensor, torch.Tensor | None]:
     """Launch the forward kernel; returns (out [B, C, N], total [B, N] or None).
 
@@ -255,7 +256,9 @@ def raymarch_forward(
     `quad` the volume's quad-layout copy (`quad_volume`), read instead of
     `vol` when given. The learned proposal, and an occupancy skip built with
     `fused=False`, are applied through per-ray windows (`skip_windows`);
-    `windows` passes windows computed earlier."""
+    `windows` passes windows computed earlier. `fwd_mode` 1 selects the
+    TMA-staged forward (a measured variant: f32, one channel, no skipping)
+    and `texture` the texture-filtered one (`TextureVolume`)."""
     _check_inputs(vol, lab, M, src, tgt, step, n_samples, n_classes)
     vol, lab, M, src, tgt, step = _prep(vol, lab, M, src, tgt, step)
     B, N, _ = tgt.shape
@@ -284,6 +287,7 @@ def raymarch_forward(
         a.sample_window = _ptr(windows)
     if quad is not None and quad.numel():
         a.vol_quad = quad.data_ptr()
+    a.fwd_mode = int(fwd_mode)
     if texture is not None:
         if texture.shape != tuple(vol.shape) or texture.device != vol.device or not texture.handle:
             raise ValueError("the texture was made from another volume or device, or is closed")

@@ -461,3 +461,17 @@ def test_texture_filtered_forward_variant_is_close():
     tex.close()
     with pytest.raises(ValueError):
         raymarch_forward(v, v, t(M), t(src), t(tgt), t(step), n, 1, width, texture=tex)
+
+
+@pytest.mark.parametrize("seed,vol_shape", [(61, (40, 36, 44)), (62, (70, 52, 64))])
+def test_tma_staged_forward_variant_is_bitwise_the_default(seed, vol_shape):
+    """The TMA variant gathers the same corners from shared-memory boxes (TMA
+    zero fill outside the volume = zero padding) with the same arithmetic."""
+    n = 230
+    vol, lab, M, src, tgt, step, width = _random_case(seed, B=3, Hd=24, Wd=32, vol_shape=vol_shape)
+    t = lambda a: torch.from_numpy(a).to(DEV)  # noqa: E731
+    v = t(vol)
+    ref, _ = raymarch_forward(v, v, t(M), t(src), t(tgt), t(step), n, 1, width, tile=(16, 8, 1))
+    out, _ = raymarch_forward(v, v, t(M), t(src), t(tgt), t(step), n, 1, width, fwd_mode=1)
+    assert torch.isfinite(out).all()
+    assert torch.equal(out, ref)
