@@ -64,6 +64,8 @@ def parse_args():
     p.add_argument("--no-batched", action="store_true", help="skip the uneven batched-launch measurement")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the per-label forward and the 1024^2 learned-proposal measurements")
+    p.add_argument("--no-graph", action="store_true",
+                   help="time eager steps only (no CUDA-graph capture; for profilers that cannot follow a capture)")
     return p.parse_args()
 
 
@@ -290,13 +292,18 @@ def run_ours(args, world, rank, local):
     for name, skip in skips.items():
         for vg in (True, False):
             key = f"{name}{'' if vg else '_pose_only'}"
-            t = timed(graphed(skip, vg).replay, args.steps)
-            table[key] = round(B * args.steps * world / t, 2)
             t = timed(make_step(skip, vg), args.steps)
             eager[key] = round(B * args.steps * world / t, 2)
+            if not args.no_graph:
+                t = timed(graphed(skip, vg).replay, args.steps)
+            table[key] = round(B * args.steps * world / t, 2)
     # headline last, with the clocks still sampling
-    head_step = graphed(skips[headline], True)
-    t_dev = timed(head_step.replay, args.steps)
+    if args.no_graph:
+        head_step = None
+        t_dev = timed(make_step(skips[headline], True), args.steps)
+    else:
+        head_step = graphed(skips[headline], True)
+        t_dev = timed(head_step.replay, args.steps)
     clk = clocks.stop()
     frames = B * args.steps * world
     value = frames / t_dev
@@ -306,7 +313,7 @@ def run_ours(args, world, rank, local):
     # loss + pose gradients go back to pinned host memory.
     host_params = torch.zeros(B, 6, pin_memory=True)
     host_out = torch.zeros(1 + B * 6, pin_memory=True)
-    step = head_step
+    eager_step = make_step(skips[headline], True)
     barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -315,8 +322,12 @@ def run_ours(args, world, rank, local):
             p = host_params.to(dev, non_blocking=True)
             reg._rot.copy_(p[:, :3])
             reg._xyz.copy_(p[:, 3:])
-        loss = step.replay()
-        g_rot, g_xyz = step.grads[0], step.grads[1]
+        if head_step is not None:
+            loss = head_step.replay()
+            g_rot, g_xyz = head_step.grads[0], head_step.grads[1]
+        else:
+            loss = eager_step().detach()
+            g_rot, g_xyz = reg._rot.grad, reg._xyz.grad
         res = torch.cat([loss[None], g_rot.flatten(), g_xyz.flatten()])
         host_out.copy_(res, non_blocking=True)
         torch.cuda.current_stream().synchronize()
@@ -462,7 +473,8 @@ def run_ours(args, world, rank, local):
             "workload": (
                 f"registration step: {args.volume} f32 phantom ({args.spacing} mm), {B} poses x "
                 f"{Hd}x{Hd} detector ({args.pixel} mm), {S} samples/ray, fwd + NCC + bwd to se(3) "
-                "6-vector and volume, the whole step replayed from a CUDA graph"
+                "6-vector and volume, " + ("eager steps" if args.no_graph else
+                                          "the whole step replayed from a CUDA graph")
             ),
             "method": f"{headline} ({'learned proposal + occupancy check' if headline == 'learned' else headline})",
             "l2": "inputs larger than L2 (volume and its gradient 512 MiB each)",

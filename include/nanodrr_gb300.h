@@ -186,7 +186,9 @@ typedef struct ndrr_raymarch_args {
     int32_t slab_mib;       /* gvol_mode 3 (and auto): quad-gradient MiB per
                                slab (0 default = 96, at most 4096)              */
     int32_t fwd_mode;       /* NDRR_FWD_* (0 default)                          */
-    int32_t pad0;
+    int32_t gvol_overwrite; /* quad layout only: 1 = the adjoint writes gvol
+                               instead of accumulating into it (no zeroing
+                               needed); rejected without vol_quad              */
     /* Texture-filtered forward (a measured variant, not the default): a
      * handle from ndrr_texture_create. When set, ndrr_raymarch_fwd samples
      * it with the texture unit's trilinear filter, whose interpolation

@@ -91,7 +91,7 @@ class RaymarchArgs(ctypes.Structure):
         ("brick_cap", ctypes.c_int32),
         ("slab_mib", ctypes.c_int32),
         ("fwd_mode", ctypes.c_int32),
-        ("pad0", ctypes.c_int32),
+        ("gvol_overwrite", ctypes.c_int32),
         ("vol_texture", ctypes.c_uint64),
     ]
 

@@ -72,11 +72,11 @@ cudaError_t launch_bwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaS
         if (gvol && ls.slab) {
             // slab-ordered adjoint: writes gM itself (ndrr_slab.cu)
             e = launch_bwd_slab(a, ls, p, st);
-            if (e == cudaSuccess) e = launch_quad_fold(a.gvol_quad, a.D, a.H, a.W, a.gvol, st);
+            if (e == cudaSuccess) e = launch_quad_fold(a.gvol_quad, a.D, a.H, a.W, a.gvol, a.gvol_overwrite != 0, st);
             return e;
         }
         e = launch_bwd_quad(p, a.vol_dtype, multi, gvol, gcam, skip, grid, block, bwd_smem_bytes(a, ls), st);
-        if (e == cudaSuccess && gvol) e = launch_quad_fold(a.gvol_quad, a.D, a.H, a.W, a.gvol, st);
+        if (e == cudaSuccess && gvol) e = launch_quad_fold(a.gvol_quad, a.D, a.H, a.W, a.gvol, a.gvol_overwrite != 0, st);
     } else if (gvol && ls.brick) {
         e = launch_brick(a, ls, p, grid, block, st);
     } else {

@@ -101,6 +101,8 @@ int32_t validate_common(const ndrr_raymarch_args* a) {
         return fail(NDRR_ERR_INVALID_ARGUMENT, "sample_window and skip_mode are exclusive (one skip at a time)");
     if (a->vol_quad != nullptr && (long long)(a->D + 4) * (a->H + 3) * (a->W + 3) >= kInt32Max)
         return fail(NDRR_ERR_LIMIT, "quad layout of a %dx%dx%d volume exceeds int32 indexing", a->D, a->H, a->W);
+    if (a->gvol_overwrite != 0 && (a->gvol_overwrite != 1 || a->vol_quad == nullptr))
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_overwrite is 0, or 1 with the quad layout");
     if (a->fwd_mode != NDRR_FWD_DEFAULT && a->fwd_mode != NDRR_FWD_TMA)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "fwd_mode must be 0 or 1 (got %d)", a->fwd_mode);
     if (a->gvol_mode < NDRR_GVOL_AUTO || a->gvol_mode > NDRR_GVOL_SLAB)

@@ -824,7 +824,7 @@ cudaError_t launch_fwd_quad(const MarchParams& p, int vol_dtype, bool multi, int
                             unsigned block, size_t smem, cudaStream_t st);
 cudaError_t launch_bwd_quad(const MarchParams& p, int vol_dtype, bool multi, bool gvol, bool gcam, int skip,
                             unsigned grid, unsigned block, size_t smem, cudaStream_t st);
-cudaError_t launch_quad_fold(const float* gquad, int D, int H, int W, float* gvol, cudaStream_t st);
+cudaError_t launch_quad_fold(const float* gquad, int D, int H, int W, float* gvol, bool overwrite, cudaStream_t st);
 cudaError_t launch_quad_build(const void* vol, int dtype, int D, int H, int W, void* quad, cudaStream_t st);
 
 MarchParams make_params(const ndrr_raymarch_args& a, const LaunchShape& ls);

@@ -53,6 +53,7 @@ __global__ void quad_build_b16_kernel(const uint16_t* __restrict__ v, int D, int
 // One CTA per (z, y) line of the volume, four consecutive x per thread: the
 // five quad entries of each of the two quad rows a thread needs are 16-byte
 // loads, and no 64-bit index division is needed.
+template <bool OVERWRITE>
 __global__ void __launch_bounds__(128) quad_fold_kernel(const float4* __restrict__ gq, int D, int H, int W,
                                                         float* __restrict__ gvol) {
     const int QX = W + 3, QY = H + 3;
@@ -75,7 +76,7 @@ __global__ void __launch_bounds__(128) quad_fold_kernel(const float4* __restrict
 #pragma unroll
         for (int j = 0; j < 4; ++j) v[j] = (a[j + 1].x + a[j].y) + (c[j + 1].z + c[j].w);
         if (vec) {
-            float4 o = *reinterpret_cast<float4*>(out + x0);
+            float4 o = OVERWRITE ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<float4*>(out + x0);
             o.x += v[0];
             o.y += v[1];
             o.z += v[2];
@@ -84,7 +85,7 @@ __global__ void __launch_bounds__(128) quad_fold_kernel(const float4* __restrict
         } else {
 #pragma unroll
             for (int j = 0; j < 4; ++j)
-                if (x0 + j < W) out[x0 + j] += v[j];
+                if (x0 + j < W) out[x0 + j] = OVERWRITE ? v[j] : out[x0 + j] + v[j];
         }
     }
 }
@@ -102,8 +103,13 @@ cudaError_t launch_quad_build(const void* vol, int dtype, int D, int H, int W, v
     return cudaGetLastError();
 }
 
-cudaError_t launch_quad_fold(const float* gquad, int D, int H, int W, float* gvol, cudaStream_t st) {
-    quad_fold_kernel<<<(unsigned)((long long)D * H), 128, 0, st>>>((const float4*)gquad, D, H, W, gvol);
+cudaError_t launch_quad_fold(const float* gquad, int D, int H, int W, float* gvol, bool overwrite,
+                             cudaStream_t st) {
+    const unsigned grid = (unsigned)((long long)D * H);
+    if (overwrite)
+        quad_fold_kernel<true><<<grid, 128, 0, st>>>((const float4*)gquad, D, H, W, gvol);
+    else
+        quad_fold_kernel<false><<<grid, 128, 0, st>>>((const float4*)gquad, D, H, W, gvol);
     return cudaGetLastError();
 }
 

@@ -358,9 +358,13 @@ def raymarch_backward(
         go = go.float()
     empty = torch.empty(0, device=dev, dtype=torch.float32)
     gM = torch.empty(B, 3, 4, device=dev, dtype=torch.float32)
+    quad_on = quad is not None and quad.numel() > 0
+    overwrite = False
     if need_gvol:
         if gvol is None:
-            gvol = torch.zeros(vol.shape, device=dev, dtype=torch.float32)
+            # with the quad layout the fold writes every voxel: no zeroing
+            overwrite = quad_on
+            gvol = (torch.empty if overwrite else torch.zeros)(vol.shape, device=dev, dtype=torch.float32)
         elif gvol.shape != vol.shape or gvol.dtype != torch.float32 or not gvol.is_contiguous():
             raise ValueError("gvol must be a contiguous float32 tensor shaped like the volume")
     else:
@@ -390,7 +394,8 @@ def raymarch_backward(
     if windows is not None:
         a.sample_window = _ptr(windows)
     gq = None
-    if quad is not None and quad.numel():
+    a.gvol_overwrite = int(overwrite)
+    if quad_on:
         a.vol_quad = quad.data_ptr()
         if need_gvol:
             D, H, W = vol.shape
