@@ -367,6 +367,9 @@ typedef struct ndrr_request {
     float* gsrc;                /* [1 | N, 3] when need_gcam                    */
     float* gtgt;                /* [N, 3] when need_gcam                        */
     float* gstep;               /* [N] when need_gcam                           */
+    const void* vol_quad;       /* quad-layout copy of vol (ndrr_quad_build) or
+                                   NULL: the request's samples read it instead
+                                   of vol (same results)                        */
 } ndrr_request;
 
 typedef struct ndrr_batch_args {

@@ -59,16 +59,18 @@ class Autotuner:
         return statistics.median(ts)
 
     def best_shape(self, vol, lab, M, src, tgt, step, n_samples, n_classes, width,
-                   candidates=SINGLE_CANDIDATES) -> tuple[int, int, int]:
-        """Fastest (tile_w, tile_h, sample_split) for these rays (cached)."""
+                   candidates=SINGLE_CANDIDATES, quad=None) -> tuple[int, int, int]:
+        """Fastest (tile_w, tile_h, sample_split) for these rays (cached),
+        timed on the quad layout when `quad` is given."""
         B, N, _ = tgt.shape
-        k = self.key(vol, n_classes, B, N, width, n_samples, candidates)
+        k = self.key(vol, n_classes, B, N, width, n_samples, candidates) + (":q" if quad is not None else "")
         if k in self.cache:
             return tuple(self.cache[k])
         timings = {}
         for shape in candidates:
             timings[shape] = self._time(
-                lambda: raymarch_forward(vol, lab, M, src, tgt, step, n_samples, n_classes, width, tile=shape)
+                lambda: raymarch_forward(vol, lab, M, src, tgt, step, n_samples, n_classes, width, tile=shape,
+                                         quad=quad)
             )
         best = min(timings, key=timings.get)
         self.cache[k] = list(best)

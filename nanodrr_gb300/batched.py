@@ -12,7 +12,9 @@ batch there is a Python loop of launches.
 
 Work order: requests are sorted by cost (rays x samples) so the largest tiles
 are taken first and the end of the launch is made of small ones. Tile shapes
-come from the autotuner (or a default).
+come from the autotuner (or a default). With `layout="quad"` (the default)
+each subject's quad-layout copy is built once (cached on the subject) and
+the requests are marched from it.
 """
 
 from __future__ import annotations
@@ -26,7 +28,7 @@ import torch
 from . import _ffi
 from .autotune import BATCHED_CANDIDATES, Autotuner
 from .raymarch import ndrr_dtype
-from .renderer import _affine_product, _make_src, _make_tgt, compact_label
+from .renderer import _affine_product, _make_src, _make_tgt, cached_quad, compact_label
 
 
 class Request(ctypes.Structure):
@@ -55,6 +57,7 @@ class Request(ctypes.Structure):
         ("gsrc", ctypes.c_void_p),
         ("gtgt", ctypes.c_void_p),
         ("gstep", ctypes.c_void_p),
+        ("vol_quad", ctypes.c_void_p),
     ]
 
 
@@ -100,7 +103,7 @@ class BatchedRenderer:
     """Static-buffer batched renderer; see the module docstring."""
 
     def __init__(self, requests: list[RenderRequest], n_classes: int = 1, autotuner: Autotuner | None = None,
-                 default_shape=(16, 16, 1), device=None):
+                 default_shape=(16, 16, 1), device=None, layout: str = "quad"):
         if not requests:
             raise ValueError("no requests")
         self.device = torch.device(device or requests[0].subject.image.device)
@@ -132,6 +135,10 @@ class BatchedRenderer:
         self.w2v = torch.stack([r.subject.world_to_voxel.float()[:3] for r in requests]).to(self.device)
         self.labs = [compact_label(r.subject) if n_classes > 1 else v for r, v in zip(requests, vols)]
         self.vols = vols
+        if layout not in ("quad", "plain"):
+            raise ValueError(f"layout must be 'quad' or 'plain', got {layout!r}")
+        # one quad-layout copy per distinct subject (cached on the subject)
+        self.quads = [cached_quad(r.subject, v) if layout == "quad" else None for r, v in zip(requests, vols)]
         # launch shapes
         shapes = []
         for i, r in enumerate(requests):
@@ -141,7 +148,7 @@ class BatchedRenderer:
                 shapes.append(autotuner.best_shape(
                     vols[i], self.labs[i], self._center_pose_M(i)[None].contiguous(),
                     self.src[i], self.tgt[i], self.step[i], r.n_samples, n_classes, r.width,
-                    candidates=BATCHED_CANDIDATES,
+                    candidates=BATCHED_CANDIDATES, quad=self.quads[i],
                 ))
         self.shapes = shapes
         # work order: most expensive first
@@ -176,6 +183,7 @@ class BatchedRenderer:
             q.go = self.go_flat.data_ptr() + int(self.offsets[i]) * es
             q.gM = self.gM[i].data_ptr()
             q.gsrc = self.gsrc[i].data_ptr()
+            q.vol_quad = self.quads[i].data_ptr() if self.quads[i] is not None else None
         tiles = (ctypes.c_int32 * R)()
         lib = _ffi.load()
         _ffi.check(lib.ndrr_batch_validate(arr, R, self.C, tiles), "ndrr_batch_validate")

@@ -5,7 +5,8 @@
 // adjoint tile body as the single-request kernels. Work items are numbered in
 // request order; callers put the most expensive requests first so the tail
 // of the launch is made of small tiles. No waits: a CTA exits when the
-// counter passes the last item.
+// counter passes the last item. A request with a quad-layout copy of its
+// volume is marched from it (the choice is made per work item).
 #include "ndrr_march.cuh"
 
 namespace ndrr {
@@ -59,6 +60,8 @@ __device__ __forceinline__ MarchParams request_params(const BatchParams& bp, con
     p.th = q.tile_h;
     p.K = q.sample_split;
     p.tm = make_tilemap(q.N, q.width, q.tile_w, q.tile_h);
+    p.quad = q.vol_quad;
+    p.qg = make_quadgeom(q.D, q.H, q.W);
     return p;
 }
 
@@ -73,7 +76,10 @@ __global__ void __launch_bounds__(256, 4) batched_fwd_kernel(const BatchParams b
         if (item >= bp.total) break;
         const int r = find_request(bp.off, bp.n_req, item);
         const MarchParams p = request_params(bp, bp.req[r], r);
-        fwd_body<VT, VT, MULTI, 0>(p, item - __ldg(bp.off + r), 0);
+        if (p.quad != nullptr)
+            fwd_body<VT, VT, MULTI, 0, true>(p, item - __ldg(bp.off + r), 0);
+        else
+            fwd_body<VT, VT, MULTI, 0, false>(p, item - __ldg(bp.off + r), 0);
     }
 }
 
@@ -89,7 +95,10 @@ __global__ void __launch_bounds__(256, 2) batched_bwd_kernel(const BatchParams b
         const int r = find_request(bp.off, bp.n_req, item);
         const MarchParams p = request_params(bp, bp.req[r], r);
         const int tile = item - __ldg(bp.off + r);
-        bwd_body<VT, MULTI, false, GCAM, 0>(p, tile, 0, (size_t)tile);
+        if (p.quad != nullptr)
+            bwd_body<VT, MULTI, false, GCAM, 0, true>(p, tile, 0, (size_t)tile);
+        else
+            bwd_body<VT, MULTI, false, GCAM, 0, false>(p, tile, 0, (size_t)tile);
     }
 }
 

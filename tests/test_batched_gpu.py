@@ -33,10 +33,11 @@ def _requests(n=9, C=1, seed=0):
     return reqs, poses
 
 
+@pytest.mark.parametrize("layout", ["quad", "plain"])
 @pytest.mark.parametrize("C", [1, 8])
-def test_batched_matches_single_requests(C):
+def test_batched_matches_single_requests(C, layout):
     reqs, poses = _requests(C=C)
-    br = BatchedRenderer(reqs, n_classes=C)
+    br = BatchedRenderer(reqs, n_classes=C, layout=layout)
     br.set_poses(poses)
     br.forward()
     for i, r in enumerate(reqs):
@@ -44,8 +45,12 @@ def test_batched_matches_single_requests(C):
         vol = br.vols[i]
         M = br.M[i : i + 1]
         out, _ = raymarch_forward(vol, br.labs[i], M, br.src[i], br.tgt[i], br.step[i], r.n_samples, C, r.width,
-                                  tile=shape)
+                                  tile=shape, quad=br.quads[i])
         assert torch.equal(br.output(i).reshape(out.shape), out), i
+        if layout == "quad":  # the quad layout holds exact copies: the plain march's image too
+            plain, _ = raymarch_forward(vol, br.labs[i], M, br.src[i], br.tgt[i], br.step[i], r.n_samples, C,
+                                        r.width, tile=shape)
+            assert torch.equal(plain, out), i
     # pose adjoint
     for i in range(len(reqs)):
         br.go(i).copy_(torch.randn_like(br.go(i)))
@@ -53,7 +58,8 @@ def test_batched_matches_single_requests(C):
     for i, r in enumerate(reqs):
         go = br.go(i).reshape(1, C, -1)
         _, gM, *_ = raymarch_backward(go, br.vols[i], br.labs[i], br.M[i : i + 1], br.src[i], br.tgt[i],
-                                      br.step[i], r.n_samples, C, r.width, False, False, tile=br.shapes[i])
+                                      br.step[i], r.n_samples, C, r.width, False, False, tile=br.shapes[i],
+                                      quad=br.quads[i])
         assert torch.equal(br.gM[i], gM[0]), i
 
 

@@ -137,7 +137,7 @@ def test_status_codes_map_to_reference_exceptions(lib):
 def test_batch_validation_is_host_only_and_counts_tiles(lib):
     from nanodrr_gb300.batched import BatchArgs, Request
 
-    assert ctypes.sizeof(Request) == 136
+    assert ctypes.sizeof(Request) == 144
     assert ctypes.sizeof(BatchArgs) == 88
     arr = (Request * 2)()
     for q, (n, w) in zip(arr, ((256 * 256, 256), (200 * 200, 200))):
