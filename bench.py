@@ -500,9 +500,10 @@ def run_ours(args, world, rank, local):
         "samples_per_s": round(n_samp * args.steps * world / t_dev, 1),
         "roofline": roofline,
         "e2e": e2e,
-        # per step: [window kernel (learned)], forward march, slab plan, scan
-        # and fill, adjoint march, per-pose reduction, quad-gradient fold
-        "gpu_launches": (8 if headline == "learned" else 7) * args.steps,
+        # per step: [window kernel (learned)], forward march, NCC moments,
+        # statistics, score and adjoint, slab plan, scan and fill, adjoint
+        # march, per-pose reduction, quad-gradient fold
+        "gpu_launches": (12 if headline == "learned" else 11) * args.steps,
         "clocks": clk,
     }
     if cpu is not None:
