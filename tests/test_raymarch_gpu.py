@@ -475,3 +475,48 @@ def test_tma_staged_forward_variant_is_bitwise_the_default(seed, vol_shape):
     out, _ = raymarch_forward(v, v, t(M), t(src), t(tgt), t(step), n, 1, width, fwd_mode=1)
     assert torch.isfinite(out).all()
     assert torch.equal(out, ref)
+
+
+def test_rays_that_miss_the_volume_on_every_path():
+    """Every ray passes beside the volume: zero images and gradients from the
+    default, slab-ordered, TMA and texture paths (empty work lists, no chunk)."""
+    from nanodrr_gb300.raymarch import TextureVolume, quad_volume
+
+    n = 120
+    vol, lab, M, src, tgt, step, width = _random_case(71, B=2, Hd=16, Wd=16, vol_shape=(24, 20, 28))
+    M = M.copy()
+    M[:, :, 3] += 1000.0  # shift every ray far outside the box
+    t = lambda a: torch.from_numpy(a).to(DEV)  # noqa: E731
+    v = t(vol)
+    q = quad_volume(v)
+    args = (v, v, t(M), t(src), t(tgt), t(step), n, 1, width)
+    out, _ = raymarch_forward(*args, quad=q)
+    assert float(out.abs().max()) == 0.0
+    tma, _ = raymarch_forward(*args, fwd_mode=1)
+    assert float(tma.abs().max()) == 0.0
+    tex = TextureVolume(v)
+    hard, _ = raymarch_forward(*args, texture=tex)
+    tex.close()
+    assert float(hard.abs().max()) == 0.0
+    go = torch.ones_like(out)
+    gvol, gM, *_ = raymarch_backward(go, *args, True, False, quad=q, gvol_mode=3)
+    assert float(gvol.abs().max()) == 0.0 and float(gM.abs().max()) == 0.0
+
+
+def test_quad_adjoint_accumulates_into_a_given_gradient():
+    """With a caller's gvol the adjoint adds (two calls give twice one call);
+    with none it writes a fresh one (no zeroing pass)."""
+    from nanodrr_gb300.raymarch import quad_volume
+
+    n = 150
+    vol, lab, M, src, tgt, step, width = _random_case(72, B=2, Hd=18, Wd=20)
+    t = lambda a: torch.from_numpy(a).to(DEV)  # noqa: E731
+    v = t(vol)
+    q = quad_volume(v)
+    go = torch.randn(2, 1, 18 * 20, device=DEV)
+    args = (go, v, v, t(M), t(src), t(tgt), t(step), n, 1, width, True, False)
+    fresh = raymarch_backward(*args, quad=q)[0]
+    acc = torch.zeros_like(v)
+    raymarch_backward(*args, quad=q, gvol=acc)
+    raymarch_backward(*args, quad=q, gvol=acc)
+    assert rel_maxabs(acc, 2 * fresh) < 1e-5
