@@ -455,7 +455,8 @@ NDRR_API int32_t ndrr_proposal_dataset(const ndrr_raymarch_args* rays, const flo
                                        float* features, float* targets, uint8_t* valid, void* stream);
 
 /* Forward, asymmetric loss (clipping the target interval costs `alpha` times
- * more than widening it) and backward over n rays; ACCUMULATES the gradient
+ * more than widening it; for an empty target, t0 > t1, only a proposed
+ * non-empty window costs) and backward over n rays; ACCUMULATES the gradient
  * of inv_count * sum(loss) into grads [NDRR_PROPOSAL_PARAMS] and the loss
  * into *loss. */
 NDRR_API int32_t ndrr_proposal_train_step(const float* params, const float* features, const float* targets,

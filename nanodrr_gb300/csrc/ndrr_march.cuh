@@ -167,12 +167,15 @@ __device__ __forceinline__ bool apply_skip(const MarchParams& p, ThreadRay& tr, 
         tn = pn - p.margin * p.inv_s;
         tf = pf + p.margin * p.inv_s;
         float unused;
-        if (first_occupied(p.occ, r, tb0, fminf(tn, tb1), kSkipSteps, &unused) != 0) return true;
-        if (first_occupied(p.occ, r, tb1, fmaxf(tf, tb0), kSkipSteps, &unused) != 0) return true;
         if (tn > tf) {
+            // Proposed empty: the two outer segments cover the whole window,
+            // so one walk over it decides.
+            if (first_occupied(p.occ, r, tb0, tb1, kSkipSteps, &unused) != 0) return true;
             r.hi = r.lo;
             return false;
         }
+        if (first_occupied(p.occ, r, tb0, fminf(tn, tb1), kSkipSteps, &unused) != 0) return true;
+        if (first_occupied(p.occ, r, tb1, fmaxf(tf, tb0), kSkipSteps, &unused) != 0) return true;
     }
     // Keep one extra sample on each side of [tn, tf].
     const float a = fminf(fmaxf(floorf(tn * sm1) - 1.0f, (float)r.lo), (float)r.hi);

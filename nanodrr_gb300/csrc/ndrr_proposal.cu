@@ -92,12 +92,15 @@ __global__ void __launch_bounds__(128) proposal_forward_kernel(const float* __re
 //   forward  h1 = relu(W1 x + b1), h2 = relu(W2 h1 + b2), y = W3 h2 + b3
 //   loss     alpha * relu(e)^2 + relu(-e)^2 per end, with e the amount by
 //            which the prediction clips the target interval (e_near =
-//            y0 - t0, e_far = t1 - y1), so clipping costs alpha times more
+//            y0 - t0, e_far = t1 - y1), so clipping costs alpha times more;
+//            relu(y1 - y0 + kEmptyMargin)^2 for a ray with an empty target
 //   backward dy, dh2 = (W3^T dy) * [h2 > 0], dh1 = (W2^T dh2) * [h1 > 0]
 //   grads    dW1 += dh1 x^T, dW2 += dh2 h1^T, dW3 += dy h2^T, db = sums
 // Each thread owns 16 entries of dW1 and of dW2 in registers across all its
 // chunks; CTA results are added to `grads` with one atomic per entry.
 constexpr int kTrainRays = 64;
+// Target gap y0 - y1 (in units of the box span) for rays with nothing to march.
+constexpr float kEmptyMargin = 0.05f;
 constexpr int kLd = 65;
 
 __global__ void __launch_bounds__(256) proposal_train_kernel(const float* __restrict__ P,
@@ -167,7 +170,17 @@ __global__ void __launch_bounds__(256) proposal_train_kernel(const float* __rest
                 y[o] = a;
             }
             float dy0 = 0.f, dy1 = 0.f;
-            if (ok) {
+            if (ok && T[r * 2 + 0] > T[r * 2 + 1]) {
+                // Empty ray: any proposal with y0 > y1 skips it whole and none
+                // clips anything, so only a proposed window (y1 > y0 -
+                // kEmptyMargin) costs, in samples of air marched.
+                const float e = y[1] - y[0] + kEmptyMargin;
+                if (e > 0.f) {
+                    lsum += e * e;
+                    dy0 = -2.f * e * inv_count;
+                    dy1 = 2.f * e * inv_count;
+                }
+            } else if (ok) {
                 const float en = y[0] - T[r * 2 + 0];  // > 0 clips the near end
                 const float ef = T[r * 2 + 1] - y[1];  // > 0 clips the far end
                 const float wn = en > 0.f ? alpha : 1.f, wf = ef > 0.f ? alpha : 1.f;

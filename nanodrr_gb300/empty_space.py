@@ -12,8 +12,8 @@ ray's box-culled range (nanodrr src/nanodrr/drr/_fused.py:144-155, 190).
   ends. It is trained on the GPU by the project's own kernels
   (`ndrr_proposal_train_step`, `ndrr_proposal_adam`) on labels the plain
   renderer itself produces (its `extent` output: first and last sample with
-  a non-zero corner), and packed to bf16 for the tensor-core inference fused
-  into the render kernels.
+  a non-zero corner), and packed to bf16 for the tensor-core inference of
+  the window kernels (`ndrr_skip_windows`).
 - `EmptySpace`: the configuration `render` reads from `subject.empty_space`.
   Mode "occupancy" marches each ray between the first and last occupied cell
   it crosses; mode "proposal" takes the network's interval when the grid

@@ -37,13 +37,16 @@ class Phantom:
         )
 
 
-def make_phantom(shape=(128, 128, 128), spacing=(1.0, 1.0, 1.0), seed: int = 0, device="cpu") -> Phantom:
-    """Phantom of `shape` = (D, H, W) voxels with (sx, sy, sz) mm spacing."""
+def make_phantom(shape=(128, 128, 128), spacing=(1.0, 1.0, 1.0), seed: int = 0, device="cpu",
+                 body_scale: float = 1.0) -> Phantom:
+    """Phantom of `shape` = (D, H, W) voxels with (sx, sy, sz) mm spacing.
+    `body_scale` < 1 shrinks the body and bones relative to the extent (more
+    air around them; 1 is the recipe)."""
     D, H, W = shape
     sx, sy, sz = spacing
     g = torch.Generator().manual_seed(seed)
     ext = torch.tensor([W * sx, H * sy, D * sz], dtype=torch.float64)
-    scale = ext / _REF_EXTENT
+    scale = ext / _REF_EXTENT * float(body_scale)
 
     def u(lo, hi, n=None):
         r = torch.rand(() if n is None else (n,), generator=g, dtype=torch.float64)

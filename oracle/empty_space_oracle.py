@@ -11,7 +11,9 @@ definitions restated here are the ones the CUDA kernels implement:
 - proposal features: entry/exit points of the footprint box (-1, dim),
   normalised by dim, with sin/cos of pi 2^k v for k = 0..3, zero-padded to 64;
 - proposal network 64-64-64-2 (ReLU) and its asymmetric loss
-  alpha * relu(e)^2 + relu(-e)^2 with e_near = y0 - t0, e_far = t1 - y1.
+  alpha * relu(e)^2 + relu(-e)^2 with e_near = y0 - t0, e_far = t1 - y1;
+  for a ray with an empty target (t0 > t1), relu(y1 - y0 + EMPTY_MARGIN)^2
+  (any proposal with y0 > y1 skips it whole, so only a proposed window costs).
 """
 
 from __future__ import annotations
@@ -19,6 +21,8 @@ from __future__ import annotations
 import numpy as np
 
 from .numpy_oracle import _rays, _taps
+
+EMPTY_MARGIN = 0.05  # target gap y0 - y1 (box-span units) for rays with nothing to march
 
 
 def occupancy_grid(vol, cell: int, max_dist: int) -> np.ndarray:
@@ -123,12 +127,16 @@ def proposal_loss_grad(P, X, T, V, alpha: float, inv_count: float) -> tuple[floa
     h1 = np.maximum(X @ W1.T + b1, 0)
     h2 = np.maximum(h1 @ W2.T + b2, 0)
     y = h2 @ W3.T + b3
+    empty = T[:, 0] > T[:, 1]
     en = y[:, 0] - T[:, 0]
     ef = T[:, 1] - y[:, 1]
     wn = np.where(en > 0, alpha, 1.0)
     wf = np.where(ef > 0, alpha, 1.0)
-    loss = float(((wn * en**2 + wf * ef**2) * V).sum() * inv_count)
-    dy = np.stack([2 * wn * en, -2 * wf * ef], 1) * (V[:, None] * inv_count)
+    ee = np.maximum(y[:, 1] - y[:, 0] + EMPTY_MARGIN, 0.0)
+    per_ray = np.where(empty, ee**2, wn * en**2 + wf * ef**2)
+    loss = float((per_ray * V).sum() * inv_count)
+    dy = np.where(empty[:, None], np.stack([-2 * ee, 2 * ee], 1), np.stack([2 * wn * en, -2 * wf * ef], 1))
+    dy = dy * (V[:, None] * inv_count)
     dh2 = (dy @ W3) * (h2 > 0)
     dh1 = (dh2 @ W2) * (h1 > 0)
     g = np.zeros(8450)
