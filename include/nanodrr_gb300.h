@@ -339,6 +339,24 @@ NDRR_API int32_t ndrr_ncc_fwd(const float* x1, const float* x2, int32_t B, int32
 NDRR_API int32_t ndrr_ncc_bwd(const float* go, const float* x1, const float* x2, const float* stats, int32_t B,
                               int32_t P, int32_t N, float* g1, float* g2, void* stream);
 
+/* ---- registration pose ------------------------------------------------------ *
+ * Replaces the reference's Registration.pose (registration/registration.py:
+ * 64-68 with geometry/se3.py:179-221, "so3_log"): the pose of each batch
+ * element is rt_inv @ pivot @ T @ pivot_inv with T = [[R, R xyz], [0, 1]] and
+ * R = exp([rot]x) (Rodrigues). rot, xyz: [B or 1, 3] float32 (rows of a
+ * single-row parameter are broadcast: pass param_rows 1); rt_inv, pivot,
+ * pivot_inv, pose: [B, 4, 4] float32, contiguous. Evaluated in float64, one
+ * thread per pose. */
+NDRR_API int32_t ndrr_pose_so3_fwd(const float* rot, const float* xyz, int32_t param_rows, const float* rt_inv,
+                                   const float* pivot, const float* pivot_inv, int32_t B, float* pose,
+                                   void* stream);
+
+/* Adjoint for gpose [B, 4, 4]: g_rot, g_xyz [B, 3] per pose (written; the
+ * caller sums the rows for a broadcast parameter). */
+NDRR_API int32_t ndrr_pose_so3_bwd(const float* gpose, const float* rot, const float* xyz, int32_t param_rows,
+                                   const float* rt_inv, const float* pivot, const float* pivot_inv, int32_t B,
+                                   float* g_rot, float* g_xyz, void* stream);
+
 /* ---- persistent batched launch -------------------------------------------- *
  * Many render requests — different volumes (same dtype), detector sizes and
  * sample counts — marched by ONE persistent kernel: CTAs take (request, tile)

@@ -344,6 +344,42 @@ int32_t ndrr_ncc_bwd(const float* go, const float* x1, const float* x2, const fl
     return ok();
 }
 
+static int32_t pose_check(const float* rot, const float* xyz, int32_t param_rows, const float* rt_inv,
+                          const float* pivot, const float* pivot_inv, int32_t B) {
+    if (B < 0) return fail(NDRR_ERR_INVALID_ARGUMENT, "B must be >= 0");
+    if (B == 0) return NDRR_OK;
+    if (!rot || !xyz || !rt_inv || !pivot || !pivot_inv)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "pose inputs must be non-NULL");
+    if (param_rows != 1 && param_rows != B)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "param_rows must be 1 or B (%d), got %d", B, param_rows);
+    return NDRR_OK;
+}
+
+int32_t ndrr_pose_so3_fwd(const float* rot, const float* xyz, int32_t param_rows, const float* rt_inv,
+                          const float* pivot, const float* pivot_inv, int32_t B, float* pose, void* stream) {
+    const int32_t rc = pose_check(rot, xyz, param_rows, rt_inv, pivot, pivot_inv, B);
+    if (rc != NDRR_OK) return rc;
+    if (B == 0) return ok();
+    if (pose == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "pose is NULL");
+    const cudaError_t e = ndrr::launch_pose_fwd(rot, xyz, param_rows, rt_inv, pivot, pivot_inv, B, pose,
+                                                reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "pose launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
+int32_t ndrr_pose_so3_bwd(const float* gpose, const float* rot, const float* xyz, int32_t param_rows,
+                          const float* rt_inv, const float* pivot, const float* pivot_inv, int32_t B, float* g_rot,
+                          float* g_xyz, void* stream) {
+    const int32_t rc = pose_check(rot, xyz, param_rows, rt_inv, pivot, pivot_inv, B);
+    if (rc != NDRR_OK) return rc;
+    if (B == 0) return ok();
+    if (!gpose || !g_rot || !g_xyz) return fail(NDRR_ERR_INVALID_ARGUMENT, "gpose, g_rot and g_xyz must be non-NULL");
+    const cudaError_t e = ndrr::launch_pose_bwd(gpose, rot, xyz, param_rows, rt_inv, pivot, pivot_inv, B, g_rot,
+                                                g_xyz, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "pose adjoint launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
 int32_t ndrr_texture_create(const float* vol, int32_t D, int32_t H, int32_t W, uint64_t* handle, void* stream) {
     if (vol == nullptr || handle == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "vol and handle must be non-NULL");
     if (D < 1 || H < 1 || W < 1 || D > 16384 || H > 16384 || W > 16384)

@@ -40,6 +40,11 @@ cudaError_t launch_ncc_fwd(const float* x1, const float* x2, int B, int P, int N
                            float* stats, void* workspace, cudaStream_t st);
 cudaError_t launch_ncc_bwd(const float* go, const float* x1, const float* x2, const float* stats, int B, int P,
                            int N, float* g1, float* g2, cudaStream_t st);
+cudaError_t launch_pose_fwd(const float* rot, const float* xyz, int param_rows, const float* rt_inv,
+                            const float* pivot, const float* pivot_inv, int B, float* pose, cudaStream_t st);
+cudaError_t launch_pose_bwd(const float* gpose, const float* rot, const float* xyz, int param_rows,
+                            const float* rt_inv, const float* pivot, const float* pivot_inv, int B, float* g_rot,
+                            float* g_xyz, cudaStream_t st);
 cudaError_t launch_homography_fwd(const float* img, const float* hom, int B, int C, int H, int W, float* out,
                                   cudaStream_t st);
 cudaError_t launch_homography_bwd(const float* go, const float* img, const float* hom, int B, int C, int H, int W,

@@ -6,9 +6,9 @@ rotation vector and translation perturb the initial pose about the
 volume's isocenter, pose = rt_inv @ pivot @ T(rot, xyz) @ pivot^-1.
 `NormalizedCrossCorrelation2d` mirrors src/nanodrr/metrics/ncc.py:8-37
 (per-image zero-mean, unit-variance correlation, optional patches).
-The pose composition is host-side torch (3x3/4x4 products); the NCC score
-and its gradient run in the library's kernels (`ndrr_ncc_fwd/bwd`), like the
-render and its adjoint. `GraphedStep` replays a whole step (pose, render,
+On CUDA the pose and its adjoint run in the library's kernels
+(`ndrr_pose_so3_fwd/bwd`), as do the NCC score and its gradient
+(`ndrr_ncc_fwd/bwd`), like the render and its adjoint. `GraphedStep` replays a whole step (pose, render,
 loss, backward) from a CUDA graph.
 """
 
@@ -45,6 +45,12 @@ class Registration(torch.nn.Module):
 
     @property
     def pose(self) -> torch.Tensor:
+        """Change of basis about the isocenter: rt_inv @ pivot @ T @ pivot_inv
+        (reference registration.py:64-68). On CUDA one kernel evaluates it
+        and its adjoint (`ndrr_pose_so3_fwd/bwd`); on the host it is composed
+        from torch ops."""
+        if self.rt_inv.is_cuda:
+            return so3_pose(self._rot, self._xyz, self.rt_inv, self.pivot, self.pivot_inv)
         T = convert(self._rot, self._xyz, "so3_log")
         return mm_small(mm_small(mm_small(self.rt_inv, self.pivot), T), self.pivot_inv)
 
@@ -52,11 +58,94 @@ class Registration(torch.nn.Module):
         return render(self.subject, self.k_inv, self.pose, self.sdd, self.height, self.width, n_samples,
                       backend=backend)
 
+    @torch.no_grad()
+    def rescale_(self, scale: float) -> None:
+        """Change the rendering resolution by rescaling the camera's
+        intrinsics (reference registration.py:70-76)."""
+        self.k_inv[..., 0, 0] /= scale
+        self.k_inv[..., 1, 1] /= scale
+        self.height = int(round(self.height * scale))
+        self.width = int(round(self.width * scale))
+
     @staticmethod
     def _make_translation(t: torch.Tensor) -> torch.Tensor:
         T = torch.eye(4, device=t.device, dtype=t.dtype)[None].repeat(len(t), 1, 1)
         T[:, :3, 3] = t
         return T
+
+
+def _pose_inputs(rot, xyz, rt_inv, pivot, pivot_inv):
+    B = rt_inv.shape[0]
+    rows = rot.shape[0]
+    if rot.shape != (rows, 3) or xyz.shape != (rows, 3) or rows not in (1, B):
+        raise ValueError(f"rot and xyz must be [1 or B, 3] with B = {B}, got {tuple(rot.shape)}, {tuple(xyz.shape)}")
+    for name, m in (("rt_inv", rt_inv), ("pivot", pivot), ("pivot_inv", pivot_inv)):
+        if m.shape != (B, 4, 4):
+            raise ValueError(f"{name} must be [{B}, 4, 4], got {tuple(m.shape)}")
+    f = lambda t: t.detach().float().contiguous()  # noqa: E731
+    return B, rows, f(rot), f(xyz), f(rt_inv), f(pivot), f(pivot_inv)
+
+
+@torch.library.custom_op("nanodrr_gb300::so3_pose", mutates_args=())
+def _so3_pose_op(rot: torch.Tensor, xyz: torch.Tensor, rt_inv: torch.Tensor, pivot: torch.Tensor,
+                 pivot_inv: torch.Tensor) -> torch.Tensor:
+    B, rows, r, x, a, p, c = _pose_inputs(rot, xyz, rt_inv, pivot, pivot_inv)
+    pose = torch.empty(B, 4, 4, device=rt_inv.device)
+    _ffi.check(_ffi.load().ndrr_pose_so3_fwd(r.data_ptr(), x.data_ptr(), rows, a.data_ptr(), p.data_ptr(),
+                                             c.data_ptr(), B, pose.data_ptr(),
+                                             torch.cuda.current_stream(rt_inv.device).cuda_stream),
+               "ndrr_pose_so3_fwd")
+    return pose.to(rt_inv.dtype)
+
+
+@_so3_pose_op.register_fake
+def _(rot, xyz, rt_inv, pivot, pivot_inv):
+    return rt_inv.new_empty(rt_inv.shape[0], 4, 4)
+
+
+@torch.library.custom_op("nanodrr_gb300::so3_pose_bwd", mutates_args=())
+def _so3_pose_bwd_op(gpose: torch.Tensor, rot: torch.Tensor, xyz: torch.Tensor, rt_inv: torch.Tensor,
+                     pivot: torch.Tensor, pivot_inv: torch.Tensor) -> tuple[torch.Tensor, torch.Tensor]:
+    B, rows, r, x, a, p, c = _pose_inputs(rot, xyz, rt_inv, pivot, pivot_inv)
+    g = gpose.float().contiguous()
+    g_rot = torch.empty(B, 3, device=rt_inv.device)
+    g_xyz = torch.empty(B, 3, device=rt_inv.device)
+    _ffi.check(_ffi.load().ndrr_pose_so3_bwd(g.data_ptr(), r.data_ptr(), x.data_ptr(), rows, a.data_ptr(),
+                                             p.data_ptr(), c.data_ptr(), B, g_rot.data_ptr(), g_xyz.data_ptr(),
+                                             torch.cuda.current_stream(rt_inv.device).cuda_stream),
+               "ndrr_pose_so3_bwd")
+    if rows == 1 and B > 1:  # a broadcast parameter: sum over the poses
+        g_rot, g_xyz = g_rot.sum(0, keepdim=True), g_xyz.sum(0, keepdim=True)
+    return g_rot, g_xyz
+
+
+@_so3_pose_bwd_op.register_fake
+def _(gpose, rot, xyz, rt_inv, pivot, pivot_inv):
+    return rot.new_empty(rot.shape, dtype=torch.float32), xyz.new_empty(xyz.shape, dtype=torch.float32)
+
+
+def _so3_pose_setup(ctx, inputs, output):
+    ctx.save_for_backward(*inputs)
+
+
+def _so3_pose_backward(ctx, gpose):
+    rot, xyz, rt_inv, pivot, pivot_inv = ctx.saved_tensors
+    if any(ctx.needs_input_grad[2:]):
+        raise RuntimeError("so3_pose differentiates the rotation and translation only; rt_inv, pivot and "
+                           "pivot_inv are fixed buffers")
+    g_rot, g_xyz = _so3_pose_bwd_op(gpose, rot, xyz, rt_inv, pivot, pivot_inv)
+    return g_rot.to(rot.dtype), g_xyz.to(xyz.dtype), None, None, None
+
+
+torch.library.register_autograd("nanodrr_gb300::so3_pose", _so3_pose_backward, setup_context=_so3_pose_setup)
+
+
+def so3_pose(rot: torch.Tensor, xyz: torch.Tensor, rt_inv: torch.Tensor, pivot: torch.Tensor,
+             pivot_inv: torch.Tensor) -> torch.Tensor:
+    """rt_inv @ pivot @ T(rot, xyz) @ pivot_inv [B, 4, 4] with T the so3_log
+    pose (R = exp([rot]x), t = R xyz), differentiable in rot and xyz
+    ([1 or B, 3]); one CUDA kernel each way (`ndrr_pose_so3_fwd/bwd`)."""
+    return _so3_pose_op(rot, xyz, rt_inv, pivot, pivot_inv)
 
 
 class NormalizedCrossCorrelation2d(torch.nn.Module):

@@ -82,7 +82,10 @@ def compact_label(subject: Subject) -> torch.Tensor:
 def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) -> torch.Tensor:
     """Adapter from the render call to the `nanodrr_gb300::fused_raymarch` op."""
     C = subject.n_classes
-    vol = subject.image[0, 0].contiguous()
+    img = subject.image
+    # A reshape of the [1, 1, D, H, W] image back-propagates as a view; an
+    # index ([0, 0]) would allocate and zero a volume-sized gradient per level.
+    vol = (img.reshape(img.shape[-3:]) if img.shape[:2] == (1, 1) else img[0, 0]).contiguous()
     lab = compact_label(subject) if C > 1 else vol
     M = _affine_product(subject.world_to_voxel.float()[:3], rt_inv.float())
     B = max(M.shape[0], tgt.shape[0])

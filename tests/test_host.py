@@ -144,3 +144,17 @@ def test_phantom_recipe_is_seeded_and_labelled():
     assert poses.shape == (4, 4, 4)
     R = poses[:, :3, :3]
     torch.testing.assert_close(R @ R.transpose(-1, -2), torch.eye(3).expand(4, 3, 3), atol=1e-5, rtol=0)
+
+
+def test_registration_rescale_scales_intrinsics_and_resolution():
+    from nanodrr_gb300.registration import Registration
+
+    sub = nd.Subject.from_volume(torch.zeros(4, 4, 4), (1.0, 1.0, 1.0), convert_to_mu=False)
+    k_inv = geometry.make_k_inv(1000.0, 1.0, 1.0, 0.0, 0.0, 100, 80)
+    rt = torch.eye(4)[None]
+    reg = Registration(sub, rt, k_inv.clone(), torch.tensor([1000.0]), 100, 80)
+    reg.rescale_(0.5)
+    assert (reg.height, reg.width) == (50, 40)
+    assert torch.allclose(reg.k_inv[0, 0, 0], k_inv[0, 0, 0] / 0.5)
+    assert torch.allclose(reg.k_inv[0, 1, 1], k_inv[0, 1, 1] / 0.5)
+    assert torch.equal(reg.k_inv[0, :, 2], k_inv[0, :, 2])

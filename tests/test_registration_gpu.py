@@ -134,3 +134,73 @@ def test_graphed_step_replays_the_eager_step():
     assert torch.equal(loss_g, ref[0])
     assert torch.equal(g_rot, ref[1]) and torch.equal(g_xyz, ref[2])  # deterministic pose gradient
     assert rel_maxabs(g_vol, ref[3]) < 1e-5  # atomics: order-dependent rounding
+
+
+def _torch_pose64(rot, xyz, rt, piv, piv_inv):
+    from nanodrr_gb300.geometry import mm_small
+
+    T = convert(rot, xyz, "so3_log")
+    return mm_small(mm_small(mm_small(rt, piv), T), piv_inv)
+
+
+@pytest.mark.parametrize("rows", [1, 5])
+@pytest.mark.parametrize("scale", [1e-8, 1e-3, 0.05, 1.2])
+def test_so3_pose_kernel_matches_torch_float64(rows, scale):
+    """ndrr_pose_so3_fwd/bwd against the torch composition of the reference's
+    Registration.pose in float64 (rotation vectors from the identity's
+    Taylor range to 1.2 rad; a broadcast single-row parameter and one row per
+    pose)."""
+    from nanodrr_gb300.registration import so3_pose
+
+    g = torch.Generator().manual_seed(int(scale * 1e9) % 1000 + rows)
+    B = 5
+    rt = phantom.random_poses(B, seed=11).double()
+    c = torch.randn(B, 3, generator=g, dtype=torch.float64) * 20
+    piv = Registration._make_translation(c)
+    piv_inv = Registration._make_translation(-c)
+    rot = (torch.randn(rows, 3, generator=g, dtype=torch.float64) * scale)
+    xyz = torch.randn(rows, 3, generator=g, dtype=torch.float64) * 5
+    gp = torch.randn(B, 4, 4, generator=g, dtype=torch.float64)
+    # float32-representable inputs: both sides see the same numbers
+    rt, piv, piv_inv, rot, xyz, gp = (t.float().double() for t in (rt, piv, piv_inv, rot, xyz, gp))
+
+    r64, x64 = rot.clone().requires_grad_(True), xyz.clone().requires_grad_(True)
+    ref = _torch_pose64(r64, x64, rt, piv, piv_inv)
+    (ref * gp).sum().backward()
+
+    rf, xf = rot.float().to(DEV).requires_grad_(True), xyz.float().to(DEV).requires_grad_(True)
+    out = so3_pose(rf, xf, rt.float().to(DEV), piv.float().to(DEV), piv_inv.float().to(DEV))
+    (out * gp.float().to(DEV)).sum().backward()
+    assert out.shape == (B, 4, 4)
+    assert rel_maxabs(out, ref.detach()) < 1e-6
+    # the kernel evaluates in float64: the gradients agree to the float32
+    # rounding of its outputs
+    assert rel_maxabs(rf.grad, r64.grad) < 1e-5
+    assert rel_maxabs(xf.grad, x64.grad) < 1e-5
+
+
+def test_so3_pose_rejects_bad_shapes():
+    from nanodrr_gb300.registration import so3_pose
+
+    rt = phantom.random_poses(3, seed=1).to(DEV)
+    piv = torch.eye(4, device=DEV).expand(3, 4, 4).contiguous()
+    with pytest.raises(ValueError):
+        so3_pose(torch.zeros(2, 3, device=DEV), torch.zeros(2, 3, device=DEV), rt, piv, piv)
+    with pytest.raises(ValueError):
+        so3_pose(torch.zeros(3, 3, device=DEV), torch.zeros(3, 3, device=DEV), rt, piv[:2], piv)
+
+
+def test_registration_pose_uses_the_kernel_and_matches_host_composition():
+    sub = _smooth_subject(size=16)
+    B = 3
+    rt = phantom.random_poses(B, seed=4).to(DEV)
+    k_inv, sdd = phantom.detector(pixel=3.0, height=8, width=8)
+    reg = Registration(sub, rt, k_inv.to(DEV), sdd.to(DEV), 8, 8, batch=B).to(DEV)
+    with torch.no_grad():
+        reg._rot.copy_(torch.tensor([[0.1, -0.2, 0.05], [0.0, 0.0, 0.0], [1e-5, 2e-5, -1e-5]], device=DEV))
+        reg._xyz.copy_(torch.tensor([[1.0, 2.0, -3.0], [0.5, 0.0, 0.0], [0.0, -1.0, 0.0]], device=DEV))
+    P = reg.pose
+    assert P.requires_grad
+    ref = _torch_pose64(reg._rot.detach().double().cpu(), reg._xyz.detach().double().cpu(),
+                        reg.rt_inv.double().cpu(), reg.pivot.double().cpu(), reg.pivot_inv.double().cpu())
+    assert rel_maxabs(P.detach(), ref) < 1e-6
