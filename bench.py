@@ -507,10 +507,11 @@ def run_ours(args, world, rank, local):
         "samples_per_s": round(n_samp * args.steps * world / t_dev, 1),
         "roofline": roofline,
         "e2e": e2e,
-        # per step: [proposal network and window check (learned)], forward
-        # march, NCC moments, statistics, score and adjoint, slab plan, scan
-        # and fill, adjoint march, per-pose reduction, quad-gradient fold
-        "gpu_launches": (13 if headline == "learned" else 11) * args.steps,
+        # per step: pose, [proposal network and window check (learned)],
+        # forward march, NCC moments, statistics, score and adjoint, slab
+        # plan, scan and fill, adjoint march, per-pose reduction,
+        # quad-gradient fold, pose adjoint
+        "gpu_launches": (15 if headline == "learned" else 13) * args.steps,
         "clocks": clk,
     }
     if cpu is not None:
