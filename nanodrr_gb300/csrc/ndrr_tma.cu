@@ -236,7 +236,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-// The driver's tensor-map encoder, looked up once (thread-safe static init).
+// The CUDA driver's tensor-map encoder, looked up once (thread-safe static init).
 static EncodeTiledFn encode_fn() {
     static const EncodeTiledFn fn = []() -> EncodeTiledFn {
         void* f = nullptr;

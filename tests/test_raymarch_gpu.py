@@ -2,7 +2,7 @@
 fixtures generated by the reference) and the float64 oracle.
 
 Mirrors the reference's parity suite (tests/drr/test_fused.py:68-226) and
-known-answer test (tests/drr/test_renderer.py:52-91), with the north-star
+known-answer test (tests/drr/test_renderer.py:52-91), with these
 tolerances: float32 forward within 1e-5 relative max-abs of the float64
 reference, gradients within 1e-3, bf16/f16 volumes within 1e-2.
 """
