@@ -50,42 +50,52 @@ __global__ void quad_build_b16_kernel(const uint16_t* __restrict__ v, int D, int
 
 // gvol[z][y][x] += the four quad entries in which voxel (x, y) of plane z is
 // a corner: (x, y) as (x0, y0), (x0 + 1, y0), (x0, y0 + 1), (x0 + 1, y0 + 1).
-// One CTA per (z, y) line of the volume, four consecutive x per thread: the
-// five quad entries of each of the two quad rows a thread needs are 16-byte
-// loads, and no 64-bit index division is needed.
+// One CTA per kFoldRows consecutive lines (z, y) of the volume, four
+// consecutive x per thread: the five quad entries of a quad row are 16-byte
+// loads, and walking down the lines each quad row is loaded once and serves
+// as the upper row of one line and the lower row of the next.
+constexpr int kFoldRows = 8;
+
 template <bool OVERWRITE>
 __global__ void __launch_bounds__(128) quad_fold_kernel(const float4* __restrict__ gq, int D, int H, int W,
                                                         float* __restrict__ gvol) {
     const int QX = W + 3, QY = H + 3;
-    const int line = blockIdx.x;  // z * H + y
-    const int z = line / H, y = line - z * H;
-    const float4* __restrict__ r0 = gq + ((size_t)(z + 2) * QY + (y + 2)) * QX;  // entries with y0 = y
-    const float4* __restrict__ r1 = r0 - QX;                                      // entries with y0 = y - 1
-    float* __restrict__ out = gvol + (size_t)line * W;
+    const int nyb = (H + kFoldRows - 1) / kFoldRows;
+    const int z = (int)(blockIdx.x / (unsigned)nyb), y0 = (int)(blockIdx.x % (unsigned)nyb) * kFoldRows;
+    const int y1 = min(H, y0 + kFoldRows);
     const bool vec = (W & 3) == 0;
     for (int x0 = threadIdx.x * 4; x0 < W; x0 += blockDim.x * 4) {
         // entries x0 + 1 .. x0 + 5 (all inside the padded row of W + 3)
-        float4 a[5], c[5];
+        int e[5];
 #pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            const int e = min(x0 + 1 + k, QX - 1);
-            a[k] = __ldg(r0 + e);
-            c[k] = __ldg(r1 + e);
-        }
-        float v[4];
+        for (int k = 0; k < 5; ++k) e[k] = min(x0 + 1 + k, QX - 1);
+        const float4* row = gq + ((size_t)(z + 2) * QY + (y0 + 1)) * QX;  // entries with y0 = y - 1
+        float4 c[5];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) v[j] = (a[j + 1].x + a[j].y) + (c[j + 1].z + c[j].w);
-        if (vec) {
-            float4 o = OVERWRITE ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<float4*>(out + x0);
-            o.x += v[0];
-            o.y += v[1];
-            o.z += v[2];
-            o.w += v[3];
-            *reinterpret_cast<float4*>(out + x0) = o;
-        } else {
+        for (int k = 0; k < 5; ++k) c[k] = __ldg(row + e[k]);
+        for (int y = y0; y < y1; ++y) {
+            row += QX;  // entries with y0 = y
+            float4 a[5];
 #pragma unroll
-            for (int j = 0; j < 4; ++j)
-                if (x0 + j < W) out[x0 + j] = OVERWRITE ? v[j] : out[x0 + j] + v[j];
+            for (int k = 0; k < 5; ++k) a[k] = __ldg(row + e[k]);
+            float v[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) v[j] = (a[j + 1].x + a[j].y) + (c[j + 1].z + c[j].w);
+            float* out = gvol + ((size_t)z * H + y) * W;
+            if (vec) {
+                float4 o = OVERWRITE ? make_float4(0.f, 0.f, 0.f, 0.f) : *reinterpret_cast<float4*>(out + x0);
+                o.x += v[0];
+                o.y += v[1];
+                o.z += v[2];
+                o.w += v[3];
+                *reinterpret_cast<float4*>(out + x0) = o;
+            } else {
+#pragma unroll
+                for (int j = 0; j < 4; ++j)
+                    if (x0 + j < W) out[x0 + j] = OVERWRITE ? v[j] : out[x0 + j] + v[j];
+            }
+#pragma unroll
+            for (int k = 0; k < 5; ++k) c[k] = a[k];
         }
     }
 }
@@ -105,7 +115,7 @@ cudaError_t launch_quad_build(const void* vol, int dtype, int D, int H, int W, v
 
 cudaError_t launch_quad_fold(const float* gquad, int D, int H, int W, float* gvol, bool overwrite,
                              cudaStream_t st) {
-    const unsigned grid = (unsigned)((long long)D * H);
+    const unsigned grid = (unsigned)((long long)D * ((H + kFoldRows - 1) / kFoldRows));
     if (overwrite)
         quad_fold_kernel<true><<<grid, 128, 0, st>>>((const float4*)gquad, D, H, W, gvol);
     else
