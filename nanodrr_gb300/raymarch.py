@@ -555,6 +555,14 @@ def fused_raymarch_ex(
     per-ray sample windows [B, N, 2] int32 the forward used, which the
     pose/camera adjoint reuses; otherwise an empty int32 tensor. `slab_mib`
     is the adjoint's slab size (0 = default), passed through to it."""
+    return fused_raymarch_ex_forward(vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid,
+                                     occ_cell, proposal, skip_mode, margin, windows_ahead, slab_mib)
+
+
+def fused_raymarch_ex_forward(vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell,
+                              proposal, skip_mode, margin, windows_ahead, slab_mib):
+    """The forward of `fused_raymarch_ex` without the op dispatch (the caller
+    uses it when no gradient is recorded and nothing is being traced)."""
     skip = _skip_of(vol, occ_grid, occ_cell, proposal, skip_mode, margin)
     windows = None
     if skip is not None and (windows_ahead or _windows_route(skip)):

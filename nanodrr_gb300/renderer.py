@@ -13,12 +13,22 @@ falling back to a CPU path.
 
 from __future__ import annotations
 
+import weakref
+
 import torch
 
-from .raymarch import fused_raymarch, fused_raymarch_ex, quad_volume
+from .raymarch import fused_raymarch, fused_raymarch_ex, fused_raymarch_ex_forward, quad_volume, raymarch_forward
 from .subject import Subject
 
 _BACKENDS = ("auto", "cuda", "triton")
+
+# Ray set-ups (src, tgt, step expanded to the batch) of recent render calls,
+# keyed by the intrinsics and sdd tensor objects: a repeated render with the
+# same camera reuses them instead of rebuilding N rays with a dozen small
+# launches. An entry is valid while both tensors are alive (weak references)
+# and unmodified (version counters).
+_RAY_CACHE: dict = {}
+_RAY_CACHE_SIZE = 4
 
 
 def fused_supported(subject: Subject, B: int, n_pixels: int) -> bool:
@@ -109,8 +119,12 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
     # traced graph cannot read: under torch.compile the plain layout is used.
     compiling = hasattr(torch, "compiler") and torch.compiler.is_compiling()
     layout = "plain" if compiling else getattr(subject, "layout", "quad")
+    # Without a recorded gradient the forward is called directly, skipping
+    # the custom op's dispatch (tens of microseconds of host time per call).
+    direct = not compiling and not (torch.is_grad_enabled() and any(
+        t.requires_grad for t in (args[0], args[2], args[3], args[4], args[5])))
     if skip is None and layout == "plain":
-        out = fused_raymarch(*args)
+        out = raymarch_forward(*args)[0] if direct else fused_raymarch(*args)
     else:
         quad = cached_quad(subject, vol) if layout == "quad" else vol.new_empty(0, dtype=torch.uint8)
         empty = vol.new_empty(0, dtype=torch.uint8)
@@ -120,7 +134,8 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
         else:
             sk = (empty, 0, empty, 0, 0.0, False)
         slab_mib = int(getattr(subject, "slab_mib", 0))
-        out = fused_raymarch_ex(args[0], quad, *args[1:], *sk, slab_mib)[0]
+        op = fused_raymarch_ex_forward if direct else fused_raymarch_ex
+        out = op(args[0], quad, *args[1:], *sk, slab_mib)[0]
     return out.reshape(B, C, height, width)
 
 
@@ -163,9 +178,45 @@ def render(
     if not rt_inv.is_cuda or not subject.image.is_cuda:
         raise RuntimeError("nanodrr_gb300 renders on CUDA devices only; move the subject and poses to a GPU")
     device, dtype = rt_inv.device, rt_inv.dtype
+    if tgt is None and src is None:
+        rays = _cached_rays(k_inv, sdd, height, width, n_samples, orthographic, rt_inv)
+        if rays is not None:
+            return render_cuda(subject, rt_inv, *rays, n_samples, height, width)
     if tgt is None:
         tgt = _make_tgt(k_inv, sdd, height, width, device, dtype)
     if src is None:
         src = _make_src(orthographic, tgt, sdd)
     step_size = (tgt - src).norm(dim=-1) / float(n_samples - 1)
     return render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width)
+
+
+def _cached_rays(k_inv, sdd, height, width, n_samples, orthographic, rt_inv):
+    """(src, tgt, step) of the render call, float32, expanded to the batch and
+    contiguous, from the ray cache or built and stored there; None when the
+    call differentiates the camera (k_inv or sdd requires a gradient) or a
+    CUDA graph is being captured without a cached entry."""
+    if k_inv.requires_grad or sdd.requires_grad:
+        return None
+    if hasattr(torch, "compiler") and torch.compiler.is_compiling():
+        return None
+    device, dtype = rt_inv.device, rt_inv.dtype
+    B = max(rt_inv.shape[0], k_inv.shape[0], sdd.shape[0])
+    key = (id(k_inv), id(sdd), height, width, n_samples, bool(orthographic), B, dtype, device)
+    hit = _RAY_CACHE.get(key)
+    if hit is not None:
+        kref, kver, sref, sver, rays = hit
+        if kref() is k_inv and sref() is sdd and kver == k_inv._version and sver == sdd._version:
+            return rays
+    if device.type == "cuda" and torch.cuda.is_current_stream_capturing():
+        return None
+    tgt = _make_tgt(k_inv, sdd, height, width, device, dtype)
+    src = _make_src(orthographic, tgt, sdd)
+    step = (tgt - src).norm(dim=-1) / float(n_samples - 1)
+    rays = (src.expand(B, -1, -1).float().contiguous(), tgt.expand(B, -1, -1).float().contiguous(),
+            step.expand(B, -1).float().contiguous())
+    for k in [k for k, v in _RAY_CACHE.items() if v[0]() is None or v[2]() is None]:
+        del _RAY_CACHE[k]  # entries whose camera tensors are gone
+    while len(_RAY_CACHE) >= _RAY_CACHE_SIZE:
+        _RAY_CACHE.pop(next(iter(_RAY_CACHE)))
+    _RAY_CACHE[key] = (weakref.ref(k_inv), k_inv._version, weakref.ref(sdd), sdd._version, rays)
+    return rays

@@ -204,3 +204,18 @@ def test_registration_pose_uses_the_kernel_and_matches_host_composition():
     ref = _torch_pose64(reg._rot.detach().double().cpu(), reg._xyz.detach().double().cpu(),
                         reg.rt_inv.double().cpu(), reg.pivot.double().cpu(), reg.pivot_inv.double().cpu())
     assert rel_maxabs(P.detach(), ref) < 1e-6
+
+
+def test_rescale_renders_at_the_new_resolution():
+    sub = _smooth_subject(size=24)
+    rt = phantom.random_poses(2, seed=5).to(DEV)
+    k_inv, sdd = phantom.detector(pixel=3.0, height=16, width=16)
+    reg = Registration(sub, rt, k_inv.to(DEV), sdd.to(DEV), 16, 16, batch=2).to(DEV)
+    with torch.no_grad():
+        a = reg(n_samples=120)
+        reg.rescale_(0.5)
+        b = reg(n_samples=120)
+        k2, _ = phantom.detector(pixel=6.0, height=8, width=8)
+        ref = nd.render(sub, k2.to(DEV), reg.pose, reg.sdd, 8, 8, n_samples=120)
+    assert a.shape[-2:] == (16, 16) and b.shape[-2:] == (8, 8)
+    assert rel_maxabs(b, ref) < 1e-5
