@@ -452,7 +452,7 @@ def run_ours(args, world, rank, local):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, sub, k_inv, sdd, rt)
-    uneven = labels = leval = sparse = None
+    uneven = labels = leval = sparse = single = None
     if not args.no_batched:
         del reg, skips
         torch.cuda.empty_cache()
@@ -464,6 +464,8 @@ def run_ours(args, world, rank, local):
         leval = learned_eval(dev)
         torch.cuda.empty_cache()
         sparse = sparse_phantom_skip(dev)
+        torch.cuda.empty_cache()
+        single = single_frame_forward(dev)
     out = {
         "metric": METRIC,
         "value": round(value, 2),
@@ -524,6 +526,8 @@ def run_ours(args, world, rank, local):
         out["learned_eval_1024"] = leval
     if sparse is not None:
         out["sparse_phantom_skip"] = sparse
+    if single is not None:
+        out["single_frame_forward"] = single
     if rank == 0:
         print(json.dumps(out), flush=True)
 
@@ -691,6 +695,57 @@ def _skip_kwargs(es, vol, M, src, tgt, step, S, det):
     if es is not None and es.mode == _ffi.NDRR_SKIP_PROPOSAL:
         return {"windows": skip_windows(vol, M, src, tgt, step, S, det, es)}
     return {"skip": es}
+
+
+def single_frame_forward(dev, runs=10, iters=100, warmup=25):
+    """The shape of the reference's published benchmark (tests/benchmark/
+    benchmark.py:23-47, 58-96): one AP pose 850 mm from the isocenter, 200^2
+    detector at 2.0 mm, sdd 1020, 500 samples, fp32 forward, on the 512 x 512
+    x 400 phantom (its CT volume is not available); frames/s timed its way,
+    CUDA events around 100 back-to-back render calls, median of 10 runs, so
+    host time per call counts. Also the same call replayed from a CUDA graph."""
+    import nanodrr_gb300 as nd
+    from nanodrr_gb300 import geometry, phantom
+
+    ph = phantom.make_phantom((400, 512, 512), (0.8, 0.8, 1.0), seed=0, device=dev)
+    sub = ph.subject(device=dev)
+    del ph
+    k_inv = geometry.make_k_inv(1020.0, 2.0, 2.0, 0.0, 0.0, 200, 200).to(dev)
+    rt = geometry.make_rt_inv(torch.tensor([[0.0, 0.0, 0.0]]), torch.tensor([[0.0, 850.0, 0.0]]), "AP",
+                              isocenter=sub.isocenter.cpu()).to(dev)
+    sdd = torch.tensor([1020.0], device=dev)
+
+    def wall_us(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(runs):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(iters):
+                fn()
+            e1.record()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) / iters * 1e3)
+        return statistics.median(ts)
+
+    with torch.no_grad():
+        call = lambda: nd.render(sub, k_inv, rt, sdd, 200, 200, n_samples=500)  # noqa: E731
+        eager = wall_us(call)
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(3):
+                call()
+        torch.cuda.current_stream().wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            call()
+        graphed = wall_us(graph.replay)
+    return {"workload": "1 AP pose, 200^2 detector at 2.0 mm, 500 samples, fp32 forward, 512x512x400 phantom",
+            "render_call_us": round(eager, 1), "render_call_frames_per_s": round(1e6 / eager, 1),
+            "graph_replay_us": round(graphed, 1), "graph_replay_frames_per_s": round(1e6 / graphed, 1)}
 
 
 def sparse_phantom_skip(dev, steps=5, epochs=40, body_scale=0.4, train_poses=64):
