@@ -174,16 +174,23 @@ def _prep(vol, lab, M, src, tgt, step):
     return vol, lab, M, src, tgt, step
 
 
-def quad_volume(vol: torch.Tensor) -> torch.Tensor:
+def quad_volume(vol: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
     """Quad-layout copy of a [D, H, W] volume (see ndrr_quad_build): element
     (qz, qy, qx) holds the four x/y corners of a cell of plane qz - 2, with a
-    zero border, so a trilinear sample is two vector loads."""
+    zero border, so a trilinear sample is two vector loads. `out`: an earlier
+    quad copy of a volume of the same shape and dtype, rebuilt in place."""
     if not vol.is_cuda or vol.dim() != 3 or vol.dtype not in _FLOAT_DTYPES:
         raise ValueError("quad_volume needs a [D, H, W] float CUDA tensor")
     vol = vol.contiguous()
     D, H, W = vol.shape
     es = 16 if vol.dtype == torch.float32 else 8
-    q = torch.empty((D + 4) * (H + 3) * (W + 3) * es, device=vol.device, dtype=torch.uint8)
+    nbytes = (D + 4) * (H + 3) * (W + 3) * es
+    if out is not None:
+        if out.dtype != torch.uint8 or out.numel() != nbytes or out.device != vol.device or not out.is_contiguous():
+            raise ValueError("out is not a quad copy of a volume of this shape and dtype")
+        q = out
+    else:
+        q = torch.empty(nbytes, device=vol.device, dtype=torch.uint8)
     lib = _ffi.load()
     _ffi.check(
         lib.ndrr_quad_build(vol.data_ptr(), ndrr_dtype(vol), D, H, W, q.data_ptr(), _stream_handle(vol.device)),

@@ -20,6 +20,7 @@ import torch
 
 from . import _ffi
 from .geometry import convert, mm_small, transform_point
+from .raymarch import quad_volume
 from .renderer import render
 
 
@@ -285,6 +286,24 @@ class GraphedStep:
             self.loss = self._step()
         # the graph's own gradient tensors (a later capture may rebind .grad)
         self.grads = [p.grad for p in self.params]
+        # The quad copy of the volume the graph reads: held here (an eager
+        # render after a volume change replaces the subject's cached copy),
+        # and rebuilt in place before a replay when the volume has changed.
+        sub = reg.subject
+        cache = getattr(sub, "_ndrr_quad_cache", None)
+        self._quad = cache[1] if cache is not None else None
+        self._vol_version = sub.image._version
+
+    def _refresh_quad(self):
+        sub = self.reg.subject
+        img = sub.image
+        if self._quad is None or img._version == self._vol_version:
+            return
+        vol = (img.reshape(img.shape[-3:]) if img.shape[:2] == (1, 1) else img[0, 0]).detach().contiguous()
+        quad_volume(vol, out=self._quad)
+        self._vol_version = img._version
+        key = (vol.data_ptr(), vol._version, vol.dtype, tuple(vol.shape), vol.device)
+        object.__setattr__(sub, "_ndrr_quad_cache", (key, self._quad))
 
     def _zero(self):
         for p in self.params:
@@ -297,5 +316,6 @@ class GraphedStep:
         return loss.detach()
 
     def replay(self) -> torch.Tensor:
+        self._refresh_quad()
         self.graph.replay()
         return self.loss

@@ -193,22 +193,27 @@ def render(
 def _cached_rays(k_inv, sdd, height, width, n_samples, orthographic, rt_inv):
     """(src, tgt, step) of the render call, float32, expanded to the batch and
     contiguous, from the ray cache or built and stored there; None when the
-    call differentiates the camera (k_inv or sdd requires a gradient) or a
-    CUDA graph is being captured without a cached entry."""
+    call differentiates the camera (k_inv or sdd requires a gradient), is
+    traced, or is captured into a CUDA graph (a graph must own its rays: a
+    cache entry may be evicted and freed while the graph still replays)."""
     if k_inv.requires_grad or sdd.requires_grad:
         return None
     if hasattr(torch, "compiler") and torch.compiler.is_compiling():
         return None
     device, dtype = rt_inv.device, rt_inv.dtype
+    if device.type != "cuda" or torch.cuda.is_current_stream_capturing():
+        return None
+    stream = torch.cuda.current_stream(device)
     B = max(rt_inv.shape[0], k_inv.shape[0], sdd.shape[0])
     key = (id(k_inv), id(sdd), height, width, n_samples, bool(orthographic), B, dtype, device)
     hit = _RAY_CACHE.get(key)
     if hit is not None:
-        kref, kver, sref, sver, rays = hit
+        kref, kver, sref, sver, rays, made_on = hit
         if kref() is k_inv and sref() is sdd and kver == k_inv._version and sver == sdd._version:
+            if stream != made_on:  # keep the allocator from reusing them under this stream's kernels
+                for t in rays:
+                    t.record_stream(stream)
             return rays
-    if device.type == "cuda" and torch.cuda.is_current_stream_capturing():
-        return None
     tgt = _make_tgt(k_inv, sdd, height, width, device, dtype)
     src = _make_src(orthographic, tgt, sdd)
     step = (tgt - src).norm(dim=-1) / float(n_samples - 1)
@@ -218,5 +223,5 @@ def _cached_rays(k_inv, sdd, height, width, n_samples, orthographic, rt_inv):
         del _RAY_CACHE[k]  # entries whose camera tensors are gone
     while len(_RAY_CACHE) >= _RAY_CACHE_SIZE:
         _RAY_CACHE.pop(next(iter(_RAY_CACHE)))
-    _RAY_CACHE[key] = (weakref.ref(k_inv), k_inv._version, weakref.ref(sdd), sdd._version, rays)
+    _RAY_CACHE[key] = (weakref.ref(k_inv), k_inv._version, weakref.ref(sdd), sdd._version, rays, stream)
     return rays

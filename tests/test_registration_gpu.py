@@ -134,6 +134,20 @@ def test_graphed_step_replays_the_eager_step():
     assert torch.equal(loss_g, ref[0])
     assert torch.equal(g_rot, ref[1]) and torch.equal(g_xyz, ref[2])  # deterministic pose gradient
     assert rel_maxabs(g_vol, ref[3]) < 1e-5  # atomics: order-dependent rounding
+    # a volume update between replays (as an optimiser makes) reaches the
+    # graph: its quad copy is rebuilt in place, also after an eager render
+    # replaced the subject's cached copy
+    with torch.no_grad():
+        vol.mul_(1.5)
+        vol[:, :, 10:20] += 0.01
+    ref2 = eager()
+    with torch.no_grad():
+        vol.mul_(0.9)
+    ref3 = eager()
+    loss_3 = step.replay().clone()
+    assert torch.equal(loss_3, ref3[0])
+    assert torch.equal(step.grads[0], ref3[1]) and torch.equal(step.grads[1], ref3[2])
+    assert not torch.equal(ref2[0], ref3[0])
 
 
 def _torch_pose64(rot, xyz, rt, piv, piv_inv):
