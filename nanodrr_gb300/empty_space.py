@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import ctypes
 import math
+import weakref
 from dataclasses import dataclass
 
 import torch
@@ -42,32 +43,69 @@ def _stream(device) -> int:
     return torch.cuda.current_stream(device).cuda_stream
 
 
+def _root(t: torch.Tensor) -> torch.Tensor:
+    """The tensor whose storage and version counter a view shares."""
+    return t._base if t._base is not None else t
+
+
 @dataclass
 class OccupancyGrid:
     grid: torch.Tensor          # uint8 [gz, gy, gx] Chebyshev distance in cells (0 = occupied)
     cell: int
     volume_shape: tuple
+    max_dist: int = 16
+    # the volume the grid describes: (weak reference to its root tensor,
+    # version counter, data pointer) at the last build
+    source: tuple | None = None
 
     @classmethod
     def build(cls, vol: torch.Tensor, cell: int = 4, max_dist: int = 16) -> "OccupancyGrid":
         """Occupancy/distance grid of a [D, H, W] volume on its CUDA device."""
         if not vol.is_cuda or vol.dim() != 3:
             raise ValueError("vol must be a [D, H, W] CUDA tensor")
-        vol = vol.contiguous()
+        g = cls(torch.empty(0, dtype=torch.uint8, device=vol.device), cell, tuple(vol.shape), max_dist)
+        g._build(vol)
+        return g
+
+    def _build(self, vol: torch.Tensor) -> None:
         D, H, W = vol.shape
         lib = _ffi.load()
         gz, gy, gx = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
-        _ffi.check(lib.ndrr_occupancy_dims(D, H, W, cell, ctypes.byref(gz), ctypes.byref(gy), ctypes.byref(gx)),
-                   "ndrr_occupancy_dims")
-        grid = torch.empty(gz.value, gy.value, gx.value, dtype=torch.uint8, device=vol.device)
-        scratch = torch.empty_like(grid)
+        _ffi.check(lib.ndrr_occupancy_dims(D, H, W, self.cell, ctypes.byref(gz), ctypes.byref(gy),
+                                           ctypes.byref(gx)), "ndrr_occupancy_dims")
+        shape = (gz.value, gy.value, gx.value)
+        if tuple(self.grid.shape) != shape or self.grid.device != vol.device:
+            self.grid = torch.empty(shape, dtype=torch.uint8, device=vol.device)
+        scratch = torch.empty_like(self.grid)
+        v = vol.detach().contiguous()
         a = _ffi.OccupancyArgs()
-        a.vol, a.vol_dtype = vol.data_ptr(), ndrr_dtype(vol)
+        a.vol, a.vol_dtype = v.data_ptr(), ndrr_dtype(v)
         a.D, a.H, a.W = D, H, W
-        a.cell, a.max_dist = cell, max_dist
-        a.grid, a.scratch = grid.data_ptr(), scratch.data_ptr()
+        a.cell, a.max_dist = self.cell, self.max_dist
+        a.grid, a.scratch = self.grid.data_ptr(), scratch.data_ptr()
         _ffi.check(lib.ndrr_occupancy_build(ctypes.byref(a), _stream(vol.device)), "ndrr_occupancy_build")
-        return cls(grid, cell, (D, H, W))
+        self.volume_shape = (D, H, W)
+        r = _root(vol)
+        self.source = (weakref.ref(r), r._version, vol.data_ptr())
+
+    def describes(self, vol: torch.Tensor) -> bool:
+        """True when the grid was built from this volume (the same tensor or
+        a view of it) and the volume has not changed since."""
+        if self.source is None:
+            return False
+        ref, version, ptr = self.source
+        r = _root(vol)
+        return ref() is r and r._version == version and vol.data_ptr() == ptr
+
+    def refresh(self, vol: torch.Tensor) -> bool:
+        """Rebuild the grid (in place when the shape is unchanged) unless it
+        describes `vol`; returns whether it rebuilt. Skipping with a grid of
+        another volume, or of an earlier version of it, could drop samples
+        that are no longer empty, so the render call refreshes first."""
+        if self.describes(vol):
+            return False
+        self._build(vol)
+        return True
 
     def occupied_fraction(self) -> float:
         return float((self.grid == 0).float().mean())

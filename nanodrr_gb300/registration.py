@@ -288,22 +288,12 @@ class GraphedStep:
         self.grads = [p.grad for p in self.params]
         # The quad copy of the volume the graph reads: held here (an eager
         # render after a volume change replaces the subject's cached copy),
-        # and rebuilt in place before a replay when the volume has changed.
+        # and rebuilt in place before a replay when the volume has changed,
+        # like the empty-space grid the graph reads.
         sub = reg.subject
         cache = getattr(sub, "_ndrr_quad_cache", None)
         self._quad = cache[1] if cache is not None else None
         self._vol_version = sub.image._version
-
-    def _refresh_quad(self):
-        sub = self.reg.subject
-        img = sub.image
-        if self._quad is None or img._version == self._vol_version:
-            return
-        vol = (img.reshape(img.shape[-3:]) if img.shape[:2] == (1, 1) else img[0, 0]).detach().contiguous()
-        quad_volume(vol, out=self._quad)
-        self._vol_version = img._version
-        key = (vol.data_ptr(), vol._version, vol.dtype, tuple(vol.shape), vol.device)
-        object.__setattr__(sub, "_ndrr_quad_cache", (key, self._quad))
 
     def _zero(self):
         for p in self.params:
@@ -315,7 +305,22 @@ class GraphedStep:
         loss.backward()
         return loss.detach()
 
+    def _refresh(self):
+        sub = self.reg.subject
+        img = sub.image
+        if img._version == self._vol_version:
+            return
+        vol = img.reshape(img.shape[-3:]) if img.shape[:2] == (1, 1) else img[0, 0]
+        if self._quad is not None:
+            quad_volume(vol.detach(), out=self._quad)
+            key = (vol.data_ptr(), vol._version, vol.dtype, tuple(vol.shape), vol.device)
+            object.__setattr__(sub, "_ndrr_quad_cache", (key, self._quad))
+        skip = getattr(sub, "empty_space", None)
+        if skip is not None:
+            skip.grid.refresh(vol)
+        self._vol_version = img._version
+
     def replay(self) -> torch.Tensor:
-        self._refresh_quad()
+        self._refresh()
         self.graph.replay()
         return self.loss

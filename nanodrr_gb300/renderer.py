@@ -118,6 +118,8 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
     # The quad copy is cached by the volume's address and version, which a
     # traced graph cannot read: under torch.compile the plain layout is used.
     compiling = hasattr(torch, "compiler") and torch.compiler.is_compiling()
+    if skip is not None and not compiling:
+        skip.grid.refresh(vol)  # the grid must describe the volume rendered
     layout = "plain" if compiling else getattr(subject, "layout", "quad")
     # Without a recorded gradient the forward is called directly, skipping
     # the custom op's dispatch (tens of microseconds of host time per call).

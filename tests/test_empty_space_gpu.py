@@ -212,3 +212,26 @@ def test_render_with_learned_proposal_through_autograd():
     (img2 * w).sum().backward()
     assert rel_maxabs(img2, img) < 1e-6
     assert rel_maxabs(rt2.grad, rt1.grad) < 1e-5
+
+
+def test_render_rebuilds_a_stale_grid():
+    """A grid built before the volume changed would skip samples that are no
+    longer empty: render rebuilds it (in place) first, so skipping stays
+    exact after an in-place edit of the volume, and a grid built from a copy
+    is replaced by one of the rendered volume."""
+    ph, sub, vol, lab, M, src, tgt, step, n, det, k_inv, sdd, rt = _case(B=3)
+    sub.empty_space = EmptySpace.occupancy(vol.clone(), cell=4)
+    grid = sub.empty_space.grid
+    with torch.no_grad():
+        a = nd.render(sub, k_inv, rt, sdd, det, det, n_samples=n)
+    assert grid.describes(sub.image.reshape(sub.image.shape[-3:]))
+    buf = grid.grid
+    with torch.no_grad():
+        sub.image[..., :4, :, :] += 0.05  # content in the air beside the body
+        b = nd.render(sub, k_inv, rt, sdd, det, det, n_samples=n)
+    assert grid.grid is buf  # rebuilt in place
+    sub.empty_space = None
+    with torch.no_grad():
+        ref = nd.render(sub, k_inv, rt, sdd, det, det, n_samples=n)
+    assert not torch.equal(a, ref)
+    assert rel_maxabs(b, ref) < 1e-6
