@@ -85,17 +85,20 @@ class OccupancyGrid:
         a.grid, a.scratch = self.grid.data_ptr(), scratch.data_ptr()
         _ffi.check(lib.ndrr_occupancy_build(ctypes.byref(a), _stream(vol.device)), "ndrr_occupancy_build")
         self.volume_shape = (D, H, W)
-        r = _root(vol)
-        self.source = (weakref.ref(r), r._version, vol.data_ptr())
+        self.source = (weakref.ref(_root(vol)), vol._version, vol.data_ptr(), (D, H, W))
 
     def describes(self, vol: torch.Tensor) -> bool:
-        """True when the grid was built from this volume (the same tensor or
-        a view of it) and the volume has not changed since."""
+        """True when `vol` is the memory the grid was built from (the same
+        tensor, a view or a detached alias of it) and has not changed since
+        (version counter). While the tensor it was built from is alive that
+        memory cannot belong to another volume; once it is gone, the grid
+        is rebuilt."""
         if self.source is None:
             return False
-        ref, version, ptr = self.source
-        r = _root(vol)
-        return ref() is r and r._version == version and vol.data_ptr() == ptr
+        ref, version, ptr, shape = self.source
+        if ref() is None:
+            return False
+        return vol.data_ptr() == ptr and tuple(vol.shape) == shape and vol._version == version
 
     def refresh(self, vol: torch.Tensor) -> bool:
         """Rebuild the grid (in place when the shape is unchanged) unless it
