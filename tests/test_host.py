@@ -158,3 +158,28 @@ def test_registration_rescale_scales_intrinsics_and_resolution():
     assert torch.allclose(reg.k_inv[0, 0, 0], k_inv[0, 0, 0] / 0.5)
     assert torch.allclose(reg.k_inv[0, 1, 1], k_inv[0, 1, 1] / 0.5)
     assert torch.equal(reg.k_inv[0, :, 2], k_inv[0, :, 2])
+
+
+def test_occupancy_grid_knows_its_volume():
+    """describes(): the same memory (tensor, view or detached alias) at the
+    same version counter; an in-place edit, another tensor, or a source that
+    is gone all call for a rebuild."""
+    import weakref
+
+    from nanodrr_gb300.empty_space import OccupancyGrid
+
+    vol = torch.rand(1, 1, 6, 5, 4)
+    view = vol.reshape(6, 5, 4)
+    g = OccupancyGrid(torch.zeros(4, 4, 4, dtype=torch.uint8), 4, (6, 5, 4),
+                      source=(weakref.ref(vol), view._version, view.data_ptr(), (6, 5, 4)))
+    assert g.describes(view)
+    assert g.describes(vol.detach()[0, 0])
+    assert not g.describes(view.clone())
+    vol.add_(1.0)
+    assert not g.describes(view)
+    g.source = (weakref.ref(vol), view._version, view.data_ptr(), (6, 5, 4))
+    assert g.describes(vol.detach().reshape(6, 5, 4))
+    other = torch.rand(6, 5, 4)
+    g.source = (weakref.ref(other), other._version, other.data_ptr(), (6, 5, 4))
+    del other
+    assert not g.describes(view)
