@@ -76,3 +76,27 @@ def test_reference_arm_runs_on_rank_zero_only(tmp_path):
     world, port = 2, _free_port()
     mp.spawn(_ref_rank_main, args=(world, port, str(tmp_path)), nprocs=world, join=True)
     assert (tmp_path / "ref1.done").exists()
+
+
+def test_reference_arm_prints_the_contract_line():
+    """`bench.py --impl reference` (the reference's CPU path restated, on the
+    host cores) prints one JSON line with the benchmark's metric, a
+    cpu_baseline describing the run and an e2e entry without device copies."""
+    import json
+    import subprocess
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    r = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--steps", "1", "--warmup", "3",
+                        "--cpu-rays", "64"], capture_output=True, text=True, timeout=600, cwd=str(ROOT))
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == bench.METRIC and d["unit"] == "frames/s"
+    assert d["value"] > 0 and d["higher_is_better"] is True and d["steps"] == 1 and d["warmup"] >= 3
+    assert {"value", "unit", "cores", "kind", "sample"} <= set(d["cpu_baseline"])
+    assert d["cpu_baseline"]["value"] == d["value"]
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+    assert "workload" in d["config"]
