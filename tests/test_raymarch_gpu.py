@@ -582,3 +582,29 @@ def test_ray_cache_follows_the_camera_tensors(random32):
     rg = rt.clone().requires_grad_(True)
     e = nd.render(sub, k_inv, rg, sdd, H, W, n_samples=n)
     assert torch.equal(e.detach(), c)
+
+
+@pytest.mark.parametrize("axis_dir", [(0.3, 0.1, 0.95), (0.1, 0.3, 0.95), (0.1, 0.95, 0.3), (0.95, 0.2, 0.1)])
+def test_slab_axis_choices_equal_direct(axis_dir):
+    """Optical axes chosen so that each slab axis is used (rays mostly along z
+    give y or x slabs, others z slabs), with 1 MiB slabs: volume and pose
+    gradients equal the direct scatter."""
+    from nanodrr_gb300.raymarch import quad_volume
+
+    vol, lab, M, src, tgt, step, width = _random_case(11, B=2, Hd=20, Wd=24, vol_shape=(72, 64, 80), C=1)
+    d = np.array(axis_dir, np.float64)
+    d /= np.linalg.norm(d)
+    a = np.cross(d, [0.0, 0.0, 1.0] if abs(d[2]) < 0.9 else [1.0, 0.0, 0.0])
+    a /= np.linalg.norm(a)
+    R = np.stack([a, np.cross(d, a), d], 1)  # columns: detector u, v and the optical axis
+    for b in range(2):
+        M[b, :, :3] = (R * (1.0 + 0.1 * b)).astype(np.float32)
+    t = lambda x: torch.from_numpy(x).to(DEV)  # noqa: E731
+    v = t(vol)
+    q = quad_volume(v)
+    go = torch.randn(2, 1, 20 * 24, device=DEV)
+    args = (go, v, t(lab), t(M), t(src), t(tgt), t(step), 240, 1, width, True, False)
+    direct = raymarch_backward(*args, quad=q, gvol_mode=1)
+    slab = raymarch_backward(*args, quad=q, gvol_mode=3, slab_mib=1)
+    assert rel_maxabs(slab[0], direct[0]) < 1e-5
+    assert rel_maxabs(slab[1], direct[1]) < 1e-5
