@@ -42,7 +42,7 @@ BASELINE_HEADLINE = None  # no published number exists for this metric
 METRIC = "fwd+bwd DRR frames/s at 512^3/256^2, learned-skip vs plain kernel"
 # DRAM read + write bytes per sample of the slab-ordered adjoint kernel from
 # an ncu capture (profiles/raymarch_bwd_slab_kernel_quad_gvol_f32_384cube_8poses.md)
-SLAB_DRAM_BYTES_PER_SAMPLE = 31.66
+SLAB_DRAM_BYTES_PER_SAMPLE = 25.16
 
 
 def parse_args():
