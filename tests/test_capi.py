@@ -183,3 +183,20 @@ def test_skip_windows_validation(lib):
     assert lib.ndrr_skip_windows(ctypes.byref(a), None, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
     assert "windows is NULL" in lib.ndrr_last_error().decode()
     assert lib.ndrr_skip_windows(ctypes.byref(a), 0x7002, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+
+
+def test_pose_entry_points_validate_on_the_host(lib):
+    """ndrr_pose_so3_fwd/bwd: NULL inputs and a parameter row count other
+    than 1 or B are rejected before any launch; B = 0 is a no-op."""
+    p = 0x7000  # never dereferenced: validation fails or returns first
+    f, b = lib.ndrr_pose_so3_fwd, lib.ndrr_pose_so3_bwd
+    assert f(None, p, 1, p, p, p, 4, p, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert f(p, p, 3, p, p, p, 4, p, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert "param_rows" in lib.ndrr_last_error().decode()
+    assert f(p, p, 1, p, p, p, 4, None, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert f(p, p, 1, p, p, p, -1, p, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert f(None, None, 1, None, None, None, 0, None, None) == _ffi.NDRR_OK
+    assert b(p, p, p, 4, p, p, p, 4, None, p, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert b(None, p, p, 4, p, p, p, 4, p, p, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert b(p, p, p, 2, p, p, p, 4, p, p, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert b(None, None, None, 1, None, None, None, 0, None, None, None) == _ffi.NDRR_OK
