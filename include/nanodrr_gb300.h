@@ -10,6 +10,14 @@
  * Return value: NDRR_OK (0) or one of the NDRR_ERR_* codes below; the message
  * of the last failure on the calling thread is returned by ndrr_last_error().
  *
+ * Alignment: every device pointer must be aligned to its element size, and
+ * the arrays the kernels move 16 bytes at a time to 16 bytes: vol_quad,
+ * gvol_quad, the workspace, and gvol when the quad layout is used (the
+ * quad-gradient fold writes four floats per store). Misaligned pointers are
+ * refused with NDRR_ERR_INVALID_ARGUMENT before anything is launched.
+ * Allocations from cudaMalloc and from the torch caching allocator always
+ * qualify; offset views into a pooled buffer may not.
+ *
  * Coordinate conventions (identical to the reference renderer):
  *   - the volume is a dense row-major [D, H, W] array; voxel (x, y, z) is
  *     element (z * H + y) * W + x;
@@ -235,6 +243,15 @@ NDRR_API const char* ndrr_build_info(void);
 /* Message of the last failed call on this thread ("" if none). */
 NDRR_API const char* ndrr_last_error(void);
 
+/* Device-side error flags of this library on the current device, set by
+ * kernels that cannot return a status through a launch:
+ * NDRR_FLAG_TMA_TIMEOUT — a TMA-staged forward (NDRR_FWD_TMA) gave up waiting
+ * for a shared-memory stage; the rays of that tile were written as NaN.
+ * *flags receives the word; clear = 1 resets it. Unlike every other entry
+ * point this one synchronises: the read waits for the device's work. */
+#define NDRR_FLAG_TMA_TIMEOUT 1u
+NDRR_API int32_t ndrr_device_flags(uint32_t* flags, int32_t clear);
+
 /* Forward ray march. Replaces the custom op nanodrr::fused_raymarch
  * (reference src/nanodrr/drr/_fused.py:415-460): same inputs (vol, lab, M,
  * src, tgt, step, n_samples, n_classes, width), caller-allocated output. The
@@ -266,7 +283,8 @@ NDRR_API int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* args, void* stream)
  *     larger calls fail with NDRR_ERR_LIMIT and a message;
  *   - the array is held by every GPU that loads the library until exit;
  *   - the first call on a device looks up the array's device address (a
- *     set-up step); make that first call before any stream capture;
+ *     set-up step, repeated for a context not seen before, e.g. after
+ *     cudaDeviceReset); make that first call before any stream capture;
  *   - all calls share the array, so calls that overlap on the GPU (for
  *     example on two streams at once) race; each call writes every partial
  *     it reads, so nothing needs clearing between calls;
@@ -424,6 +442,16 @@ NDRR_API int32_t ndrr_batched_bwd(const ndrr_batch_args* args, void* stream);
 NDRR_API int32_t ndrr_quad_dims(int32_t D, int32_t H, int32_t W, int32_t* qz, int32_t* qy, int32_t* qx);
 NDRR_API int32_t ndrr_quad_build(const void* vol, int32_t vol_dtype, int32_t D, int32_t H, int32_t W, void* quad,
                                  void* stream);
+
+/* HU -> linear attenuation (1/mm) of n elements, elementwise: replaces the
+ * reference's hu_to_mu (src/nanodrr/data/preprocess.py:9-50), which Subject
+ * .image applies (src/nanodrr/data/subject.py:98-107). hu and mu: n elements
+ * of dtype (f32, f16 or bf16), device pointers; mu may alias hu. HU is
+ * clamped at -1000; at or below 0 HU mu = (hu / 1000 + 1) * mu_water, above
+ * it mu = mu_water + (hu / hu_bone) * (mu_bone - mu_water); mu is clamped at
+ * 0. Computed in fp32. */
+NDRR_API int32_t ndrr_hu_to_mu(const void* hu, int32_t dtype, int64_t n, float mu_water, float mu_bone,
+                               float hu_bone, void* mu, void* stream);
 
 /* ---- empty-space structures ---------------------------------------------- */
 typedef struct ndrr_occupancy_args {

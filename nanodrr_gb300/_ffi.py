@@ -21,6 +21,7 @@ NDRR_ERR_DTYPE = 3
 NDRR_ERR_WORKSPACE = 4
 NDRR_ERR_CUDA = 5
 NDRR_ERR_DEVICE_TIMEOUT = 6
+NDRR_FLAG_TMA_TIMEOUT = 1
 
 # ndrr_dtype
 NDRR_F32, NDRR_F16, NDRR_BF16, NDRR_U8, NDRR_I8, NDRR_I16, NDRR_I32, NDRR_I64 = range(8)
@@ -134,6 +135,7 @@ SIGNATURES: dict[str, tuple] = {
     "ndrr_abi_version": (ctypes.c_int32, []),
     "ndrr_build_info": (ctypes.c_char_p, []),
     "ndrr_last_error": (ctypes.c_char_p, []),
+    "ndrr_device_flags": (ctypes.c_int32, [ctypes.POINTER(ctypes.c_uint32), ctypes.c_int32]),
     "ndrr_raymarch_fwd": (ctypes.c_int32, [ctypes.POINTER(RaymarchArgs), ctypes.c_void_p]),
     "ndrr_raymarch_bwd_workspace_bytes": (
         ctypes.c_int32,
@@ -147,6 +149,8 @@ SIGNATURES: dict[str, tuple] = {
     "ndrr_batched_bwd": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p]),
     "ndrr_quad_dims": (ctypes.c_int32, [ctypes.c_int32] * 3 + [_i32p] * 3),
     "ndrr_quad_build": (ctypes.c_int32, [ctypes.c_void_p] + [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 2),
+    "ndrr_hu_to_mu": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
+                                       ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]),
     "ndrr_occupancy_dims": (ctypes.c_int32, [ctypes.c_int32] * 4 + [_i32p] * 3),
     "ndrr_occupancy_build": (ctypes.c_int32, [ctypes.POINTER(OccupancyArgs), ctypes.c_void_p]),
     "ndrr_skip_windows": (ctypes.c_int32, [ctypes.POINTER(RaymarchArgs), ctypes.c_void_p, ctypes.c_void_p]),

@@ -4,6 +4,8 @@
 // indexing limits of fused_supported at src/nanodrr/drr/backends.py:66-69)
 // and adds the pointer/dtype/shape checks a C caller needs. Nothing here
 // allocates device memory or synchronises.
+#include <cuda.h>
+
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
@@ -43,6 +45,59 @@ int sm_count_current() {
     if (cudaGetDevice(&dev) != cudaSuccess) return 148;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) return 148;
     return sms;
+}
+
+size_t dtype_bytes(int32_t d) {
+    switch (d) {
+        case NDRR_F32: case NDRR_I32: return 4;
+        case NDRR_F16: case NDRR_BF16: case NDRR_I16: return 2;
+        case NDRR_I64: return 8;
+        default: return 1;
+    }
+}
+
+bool misaligned(const void* p, size_t align) { return (reinterpret_cast<uintptr_t>(p) % align) != 0; }
+
+// Alignment of every pointer the kernels dereference: each element type's
+// natural alignment, and 16 bytes for the arrays read or written with
+// 16-byte vector instructions (the quad layout, its gradient scratch, and
+// the volume gradient the quad fold writes four floats at a time). A
+// misaligned vector access would end the CUDA context, so it is refused
+// here, before any launch.
+int32_t validate_alignment(const ndrr_raymarch_args* a) {
+    struct Check {
+        const void* p;
+        size_t align;
+        const char* name;
+    };
+    const size_t ve = dtype_bytes(a->vol_dtype);
+    const Check checks[] = {
+        {a->vol, ve, "vol"},
+        {a->n_classes > 1 ? a->lab : nullptr, dtype_bytes(a->lab_dtype), "lab"},
+        {a->M, 4, "M"},
+        {a->src, 4, "src"},
+        {a->tgt, 4, "tgt"},
+        {a->step, 4, "step"},
+        {a->t_window, 4, "t_window"},
+        {a->out, dtype_bytes(a->out_dtype), "out"},
+        {a->out_total, dtype_bytes(a->out_dtype), "out_total"},
+        {a->go, dtype_bytes(a->go_dtype), "go"},
+        {a->gvol, a->vol_quad != nullptr ? 16 : 4, "gvol (16 bytes with the quad layout)"},
+        {a->gM, 4, "gM"},
+        {a->gsrc, 4, "gsrc"},
+        {a->gtgt, 4, "gtgt"},
+        {a->gstep, 4, "gstep"},
+        {a->workspace, 16, "workspace"},
+        {a->skip_stats, 8, "skip_stats"},
+        {a->out_extent, 8, "out_extent"},
+        {a->vol_quad, 16, "vol_quad"},
+        {a->gvol_quad, 16, "gvol_quad"},
+        {a->sample_window, 8, "sample_window"},
+    };
+    for (const Check& c : checks)
+        if (c.p != nullptr && misaligned(c.p, c.align))
+            return fail(NDRR_ERR_INVALID_ARGUMENT, "%s must be %zu-byte aligned (got %p)", c.name, c.align, c.p);
+    return NDRR_OK;
 }
 
 // Shape/pointer checks shared by the forward and the adjoint.
@@ -95,8 +150,7 @@ int32_t validate_common(const ndrr_raymarch_args* a) {
             return fail(NDRR_ERR_INVALID_ARGUMENT, "proposal skipping needs packed proposal parameters");
         if (!(a->proposal_margin >= 0.f)) return fail(NDRR_ERR_INVALID_ARGUMENT, "proposal_margin must be >= 0");
     }
-    if (reinterpret_cast<uintptr_t>(a->sample_window) % 8 != 0)
-        return fail(NDRR_ERR_INVALID_ARGUMENT, "sample_window must be 8-byte aligned");
+    if (validate_alignment(a) != NDRR_OK) return NDRR_ERR_INVALID_ARGUMENT;
     if (a->sample_window != nullptr && a->skip_mode != NDRR_SKIP_NONE)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "sample_window and skip_mode are exclusive (one skip at a time)");
     if (a->vol_quad != nullptr && (long long)(a->D + 4) * (a->H + 3) * (a->W + 3) >= kInt32Max)
@@ -146,6 +200,15 @@ const char* ndrr_build_info(void) {
 }
 
 const char* ndrr_last_error(void) { return g_last_error.c_str(); }
+
+int32_t ndrr_device_flags(uint32_t* flags, int32_t clear) {
+    if (flags == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "flags is NULL");
+    unsigned v = 0;
+    const cudaError_t e = ndrr::device_flags(&v, clear != 0);
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "reading the device flags failed: %s", cudaGetErrorString(e));
+    *flags = v;
+    return ok();
+}
 
 int32_t ndrr_raymarch_fwd(const ndrr_raymarch_args* a, void* stream) {
     int32_t rc = validate_common(a);
@@ -413,11 +476,27 @@ int32_t ndrr_quad_dims(int32_t D, int32_t H, int32_t W, int32_t* qz, int32_t* qy
 int32_t ndrr_quad_build(const void* vol, int32_t dtype, int32_t D, int32_t H, int32_t W, void* quad, void* stream) {
     if (vol == nullptr || quad == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "vol and quad must be non-NULL");
     if (!is_float_dtype(dtype)) return fail(NDRR_ERR_DTYPE, "volume dtype %d unsupported", dtype);
+    if (misaligned(quad, 16) || misaligned(vol, dtype_bytes(dtype)))
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "quad must be 16-byte aligned and vol aligned to its element");
     int32_t qz, qy, qx;
     int32_t rc = ndrr_quad_dims(D, H, W, &qz, &qy, &qx);
     if (rc != NDRR_OK) return rc;
     const cudaError_t e = ndrr::launch_quad_build(vol, dtype, D, H, W, quad, reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "quad build failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
+int32_t ndrr_hu_to_mu(const void* hu, int32_t dtype, int64_t n, float mu_water, float mu_bone, float hu_bone,
+                      void* mu, void* stream) {
+    if (n < 0) return fail(NDRR_ERR_INVALID_ARGUMENT, "n must be >= 0 (got %lld)", (long long)n);
+    if (!is_float_dtype(dtype)) return fail(NDRR_ERR_DTYPE, "HU dtype %d unsupported (f32, f16, bf16)", dtype);
+    if (n == 0) return ok();
+    if (hu == nullptr || mu == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "hu and mu must be non-NULL");
+    if (!(hu_bone != 0.f)) return fail(NDRR_ERR_INVALID_ARGUMENT, "hu_bone must be non-zero");
+    const float dmu = (float)((double)mu_bone - (double)mu_water);
+    const cudaError_t e =
+        ndrr::launch_hu_to_mu(hu, dtype, n, mu_water, dmu, hu_bone, mu, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "HU conversion launch failed: %s", cudaGetErrorString(e));
     return ok();
 }
 
@@ -438,6 +517,8 @@ int32_t ndrr_batch_validate(const ndrr_request* q, int32_t n, int32_t n_classes,
             (r.sample_split != 1 && r.sample_split != 2 && r.sample_split != 4))
             return fail(NDRR_ERR_INVALID_ARGUMENT,
                         "request %d: tile_w (mult. of 8) * tile_h (mult. of 4) * sample_split (1/2/4) must be 256", i);
+        if (misaligned(r.vol_quad, 16))
+            return fail(NDRR_ERR_INVALID_ARGUMENT, "request %d: vol_quad must be 16-byte aligned", i);
         const ndrr::TileMap tm = ndrr::make_tilemap(r.N, r.width, r.tile_w, r.tile_h);
         tiles[i] = tm.tiles;
     }
@@ -521,26 +602,91 @@ constexpr size_t kNoAllocScratchBytes = size_t(4) << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-constexpr int kNoAllocMaxDevices = 64;
-std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+// The runtime can tear a device's context down and build a new one
+// (cudaDeviceReset), which loads this module again, possibly at another
+// address; a user can also make a context of their own current. So the
+// looked-up address is kept per (device, context id) — context ids are never
+// reused within a process — and looked up again for a context not seen
+// before. The context id comes from the driver entry points cuCtxGetCurrent
+// and cuCtxGetId, fetched through the runtime (no link to the driver
+// library); without them every call looks the address up.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
 
-// Device address of the scratch array on the current device. The host-side
+struct CtxEntryPoints {
+    CtxGetCurrentFn get_current = nullptr;
+    CtxGetIdFn get_id = nullptr;
+};
+
+const CtxEntryPoints& ctx_entry_points() {
+    static const CtxEntryPoints fns = []() {
+        CtxEntryPoints f;
+        void* a = nullptr;
+        void* b = nullptr;
+        cudaDriverEntryPointQueryResult qa, qb;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &qa) == cudaSuccess &&
+            qa == cudaDriverEntryPointSuccess &&
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &qb) == cudaSuccess &&
+            qb == cudaDriverEntryPointSuccess) {
+            f.get_current = reinterpret_cast<CtxGetCurrentFn>(a);
+            f.get_id = reinterpret_cast<CtxGetIdFn>(b);
+        }
+        return f;
+    }();
+    return fns;
+}
+
+// Id of the calling thread's current context; false when none is current
+// yet or the entry points are unavailable.
+bool current_context_id(unsigned long long* id) {
+    const CtxEntryPoints& f = ctx_entry_points();
+    if (f.get_current == nullptr || f.get_id == nullptr) return false;
+    CUcontext ctx = nullptr;
+    if (f.get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return false;
+    return f.get_id(ctx, id) == CUDA_SUCCESS;
+}
+
+struct ScratchAddress {
+    int device;
+    unsigned long long context;
+    void* ptr;
+};
+
+constexpr int kNoAllocMaxEntries = 64;
+std::mutex g_noalloc_mu;
+ScratchAddress g_noalloc_seen[kNoAllocMaxEntries];
+int g_noalloc_count = 0;
+
+// Device address of the scratch array in the current context. The host-side
 // name of a __device__ array is only a stand-in, so the address is looked up
-// with cudaGetSymbolAddress, once per device, with that device current.
+// with cudaGetSymbolAddress once per device and context, with that device
+// current (the lookup also makes the device's primary context current when
+// the thread has none yet).
 cudaError_t noalloc_scratch(void** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    unsigned long long ctx = 0;
+    bool known = current_context_id(&ctx);
     std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (g_noalloc_ptr[dev] == nullptr) {
-        void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess) return e;
-        g_noalloc_ptr[dev] = p;
+    if (known) {
+        for (int i = 0; i < g_noalloc_count; ++i) {
+            if (g_noalloc_seen[i].device == dev && g_noalloc_seen[i].context == ctx) {
+                *out = g_noalloc_seen[i].ptr;
+                return cudaSuccess;
+            }
+        }
     }
-    *out = g_noalloc_ptr[dev];
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) return e;
+    if (!known) known = current_context_id(&ctx);
+    if (known) {
+        // A full table overwrites a slot chosen by the context id (a lookup is cheap).
+        const int slot = g_noalloc_count < kNoAllocMaxEntries ? g_noalloc_count++ : (int)(ctx % kNoAllocMaxEntries);
+        g_noalloc_seen[slot] = ScratchAddress{dev, ctx, p};
+    }
+    *out = p;
     return cudaSuccess;
 }
 

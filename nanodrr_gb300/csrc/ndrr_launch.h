@@ -50,6 +50,9 @@ cudaError_t launch_homography_fwd(const float* img, const float* hom, int B, int
 cudaError_t launch_homography_bwd(const float* go, const float* img, const float* hom, int B, int C, int H, int W,
                                   float* gimg, float* ghom, float* partials, cudaStream_t st);
 cudaError_t launch_batched(const ndrr_batch_args& a, bool backward, int sm_count, cudaStream_t st);
+cudaError_t device_flags(unsigned* out, bool clear);
+cudaError_t launch_hu_to_mu(const void* hu, int dtype, long long n, float mu_water, float dmu, float hu_bone,
+                            void* mu, cudaStream_t st);
 cudaError_t launch_occupancy(const void* vol, int vol_dtype, int D, int H, int W, int cell, int max_dist,
                              uint8_t* dist, uint8_t* scratch, cudaStream_t st);
 

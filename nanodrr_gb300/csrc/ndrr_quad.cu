@@ -1,6 +1,7 @@
-// Quad volume layout: build (one pass over the padded extent) and the fold of
-// the quad-layout volume gradient back into the volume's layout. The layout
-// is defined in ndrr_device.cuh (QuadOf, make_quadgeom).
+// Volume preparation and the quad layout: the HU -> attenuation conversion,
+// the quad build (one pass over the padded extent) and the fold of the
+// quad-layout volume gradient back into the volume's layout. The layout is
+// defined in ndrr_device.cuh (QuadOf, make_quadgeom).
 #include "ndrr_march.cuh"
 
 namespace ndrr {
@@ -100,6 +101,37 @@ __global__ void __launch_bounds__(128) quad_fold_kernel(const float4* __restrict
     }
 }
 
+// HU -> linear attenuation (1/mm), the reference's piecewise-linear map
+// (nanodrr src/nanodrr/data/preprocess.py:44-50): clamp HU at -1000; at or
+// below 0 HU the air-water line (h / 1000 + 1) * mu_water, above it the
+// water-bone line mu_water + (h / hu_bone) * dmu with dmu = mu_bone -
+// mu_water; clamp at 0 (NaN passes through both clamps, as torch.clamp lets
+// it). One element per thread and grid-stride, in fp32; the
+// 16-bit types convert on load and round to nearest-even on store.
+template <typename T>
+__device__ __forceinline__ float hu_load(const T* p, long long i);
+template <>
+__device__ __forceinline__ float hu_load<float>(const float* p, long long i) { return __ldg(p + i); }
+template <>
+__device__ __forceinline__ float hu_load<__half>(const __half* p, long long i) { return __half2float(__ldg(p + i)); }
+template <>
+__device__ __forceinline__ float hu_load<__nv_bfloat16>(const __nv_bfloat16* p, long long i) {
+    return __bfloat162float(__ldg(p + i));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) hu_to_mu_kernel(const T* __restrict__ hu, long long n, float mu_water,
+                                                       float dmu, float hu_bone, T* __restrict__ mu) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float x = hu_load(hu, i);
+        const float h = x < -1000.0f ? -1000.0f : x;  // NaN stays NaN, as in torch.clamp
+        const float below = __fmul_rn(__fadd_rn(__fdiv_rn(h, 1000.0f), 1.0f), mu_water);
+        const float above = __fadd_rn(mu_water, __fmul_rn(__fdiv_rn(h, hu_bone), dmu));
+        const float m = h > 0.0f ? above : below;
+        st_out(mu, (size_t)i, m > 0.0f ? m : (m == m ? 0.0f : m));
+    }
+}
+
 static int grid_for(long long n) { return (int)std::max(1LL, std::min((n + 255) / 256, 152LL * 32)); }
 
 cudaError_t launch_quad_build(const void* vol, int dtype, int D, int H, int W, void* quad, cudaStream_t st) {
@@ -110,6 +142,24 @@ cudaError_t launch_quad_build(const void* vol, int dtype, int D, int H, int W, v
         quad_build_b16_kernel<<<grid_for(n), 256, 0, st>>>((const uint16_t*)vol, D, H, W, (uint2*)quad);
     else
         return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_hu_to_mu(const void* hu, int dtype, long long n, float mu_water, float dmu, float hu_bone,
+                            void* mu, cudaStream_t st) {
+    switch (dtype) {
+        case NDRR_F32:
+            hu_to_mu_kernel<<<grid_for(n), 256, 0, st>>>((const float*)hu, n, mu_water, dmu, hu_bone, (float*)mu);
+            break;
+        case NDRR_F16:
+            hu_to_mu_kernel<<<grid_for(n), 256, 0, st>>>((const __half*)hu, n, mu_water, dmu, hu_bone, (__half*)mu);
+            break;
+        case NDRR_BF16:
+            hu_to_mu_kernel<<<grid_for(n), 256, 0, st>>>((const __nv_bfloat16*)hu, n, mu_water, dmu, hu_bone,
+                                                         (__nv_bfloat16*)mu);
+            break;
+        default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 

@@ -11,9 +11,11 @@
 // the arithmetic is the software path's (same floor, fractions and lerps), so
 // the image is bitwise that of the plain forward.
 //
-// Waits on the mbarriers are bounded: a stage that never completes sets the
-// CTA's rays to NaN (visible to the caller) and the CTA stops after a second
-// bounded wait.
+// Waits on the mbarriers are bounded. When a stage does not complete in
+// time the CTA sets NDRR_FLAG_TMA_TIMEOUT in the library's device flags
+// (read by ndrr_device_flags), waits again, bounded, for each of its copies
+// still in flight so that none lands after the CTA's shared memory is
+// released, writes NaN for its rays and returns.
 #include <cuda.h>
 
 #include "ndrr_march.cuh"
@@ -29,6 +31,9 @@ constexpr unsigned kTBoxBytes = kTBoxElems * sizeof(float);  // 32 KB
 constexpr int kTRays = 128;                                   // 16 x 8 tile, one thread per ray
 constexpr int kTMaxChunk = 64;
 constexpr int kTWaitLimit = 1 << 24;
+
+// Library-wide device-side error flags (NDRR_FLAG_*), one word per device.
+__device__ unsigned int g_ndrr_device_flags;
 
 struct TmaShared {
     float box[2][kTBoxElems];
@@ -171,8 +176,10 @@ __global__ void __launch_bounds__(kTRays) raymarch_fwd_tma_kernel(const MarchPar
     };
 
     float acc = 0.f;
-    unsigned parity[2] = {0u, 0u};
+    unsigned parity[2] = {0u, 0u};  // phase each stage's next completion ends
     bool failed = false;
+    bool cur_pending = false;   // this thread's wait on the current stage gave up
+    bool next_planned = false;  // a copy into the other stage was issued
     int c0 = s_begin;
     if (c0 < s_end) plan(c0, 0);
     int stage = 0;
@@ -181,10 +188,15 @@ __global__ void __launch_bounds__(kTRays) raymarch_fwd_tma_kernel(const MarchPar
         const int ox = sh.origin[stage][0], oy = sh.origin[stage][1], oz = sh.origin[stage][2];
         const bool staged = sh.origin[stage][3] != 0;
         // stage the next chunk while this one is marched
-        if (c1 < s_end) plan(c1, stage ^ 1);
+        next_planned = c1 < s_end;
+        if (next_planned) plan(c1, stage ^ 1);
         if (staged) {
-            if (!bar_wait(&sh.bar[stage], parity[stage])) failed = true;
-            parity[stage] ^= 1u;
+            if (bar_wait(&sh.bar[stage], parity[stage])) {
+                parity[stage] ^= 1u;
+            } else {
+                failed = true;
+                cur_pending = true;
+            }
         }
         const int a = max(lo, c0), e = min(hi, c1);
         if (!failed) {
@@ -223,10 +235,14 @@ __global__ void __launch_bounds__(kTRays) raymarch_fwd_tma_kernel(const MarchPar
         stage ^= 1;
     }
     if (failed) {
-        // a stage never completed: wait (bounded) for the other one too, then
-        // report NaN for this tile's rays
+        // A stage did not complete in time: flag it for the host, then wait
+        // again (bounded) for the copies this thread has not seen complete —
+        // the current stage if its own wait gave up, and the other stage if
+        // a copy was issued into it — before the CTA exits; its rays read NaN.
+        if (threadIdx.x == 0) atomicOr(&g_ndrr_device_flags, (unsigned)NDRR_FLAG_TMA_TIMEOUT);
+        if (cur_pending) bar_wait(&sh.bar[stage], parity[stage]);
         const int other = stage ^ 1;
-        if (sh.origin[other][3] != 0) bar_wait(&sh.bar[other], parity[other]);
+        if (next_planned && sh.origin[other][3] != 0) bar_wait(&sh.bar[other], parity[other]);
         acc = __int_as_float(0x7fc00000);
     }
     if (n >= 0) st_out(reinterpret_cast<float*>(p.out), tr.bn, acc * tr.stepv);
@@ -276,6 +292,17 @@ cudaError_t launch_fwd_tma(const ndrr_raymarch_args& a, const LaunchShape& ls, c
     const unsigned grid = (unsigned)((size_t)a.B * p.tm.tiles);
     raymarch_fwd_tma_kernel<<<grid, kTRays, smem, st>>>(p, map);
     return cudaGetLastError();
+}
+
+// Read (and optionally clear) the device flags of the current device.
+// Synchronous: the copy waits for the device's work to finish.
+cudaError_t device_flags(unsigned* out, bool clear) {
+    cudaError_t e = cudaMemcpyFromSymbol(out, g_ndrr_device_flags, sizeof(unsigned));
+    if (e == cudaSuccess && clear) {
+        const unsigned zero = 0u;
+        e = cudaMemcpyToSymbol(g_ndrr_device_flags, &zero, sizeof(unsigned));
+    }
+    return e;
 }
 
 }  // namespace ndrr

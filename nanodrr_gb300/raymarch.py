@@ -56,6 +56,16 @@ def _ptr(t: torch.Tensor | None) -> int | None:
     return t.data_ptr()
 
 
+def device_flags(clear: bool = False) -> int:
+    """The library's device-side error flags on the current device
+    (`_ffi.NDRR_FLAG_*`; e.g. a TMA-staged forward whose stage wait gave
+    up). Synchronises the device."""
+    lib = _ffi.load()
+    v = ctypes.c_uint32(0)
+    _ffi.check(lib.ndrr_device_flags(ctypes.byref(v), int(clear)), "ndrr_device_flags")
+    return int(v.value)
+
+
 def _check_inputs(vol, lab, M, src, tgt, step, n_samples, n_classes):
     if not vol.is_cuda:
         raise RuntimeError("nanodrr_gb300 renders on CUDA devices only (got a volume on %s)" % vol.device)

@@ -259,7 +259,9 @@ class GraphedStep:
 
     `loss_fn(image, target)` returns a scalar. The pose parameters of `reg`
     (and the subject's volume, if it requires a gradient) are the graph's
-    static inputs: change them in place (`copy_`) between replays. After each
+    static inputs: change them in place (`copy_`) between replays; replacing
+    the subject's volume with another tensor makes `replay()` raise
+    RuntimeError (the graph would still read the old memory). After each
     `replay()`, `loss` holds the step's loss and `grads` (the parameters'
     `.grad` tensors at capture: pose rotation, translation, then the volume
     when it requires a gradient) its gradients, overwritten by each replay.
@@ -293,7 +295,10 @@ class GraphedStep:
         sub = reg.subject
         cache = getattr(sub, "_ndrr_quad_cache", None)
         self._quad = cache[1] if cache is not None else None
-        self._vol_version = sub.image._version
+        # The volume tensor the graph reads, held so that its memory cannot be
+        # freed and handed to another tensor while the graph can replay.
+        self._vol = sub.image
+        self._vol_version = self._vol._version
 
     def _zero(self):
         for p in self.params:
@@ -308,6 +313,12 @@ class GraphedStep:
     def _refresh(self):
         sub = self.reg.subject
         img = sub.image
+        if img.data_ptr() != self._vol.data_ptr() or img.shape != self._vol.shape or img.dtype != self._vol.dtype:
+            raise RuntimeError(
+                "the subject's volume is not the tensor this graph was captured with (a new tensor was assigned, "
+                "or the HU -> mu conversion produced a new one); build a new GraphedStep, or update the captured "
+                "volume in place instead"
+            )
         if img._version == self._vol_version:
             return
         vol = img.reshape(img.shape[-3:]) if img.shape[:2] == (1, 1) else img[0, 0]

@@ -23,7 +23,8 @@ Cases mirror the reference's own tests:
                   (src/nanodrr/metrics/ncc.py) in float64, global and 5x5
                   patches: scores and gradients to both images.
 
-Usage: python tests/golden/make_golden.py [/path/to/reference] [case ...]
+Usage: python tests/golden/make_golden.py /path/to/reference [case ...]
+(or NANODRR_REFERENCE=/path/to/reference python tests/golden/make_golden.py)
 """
 
 from __future__ import annotations
@@ -34,7 +35,12 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parents[1]
-REF = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+if len(sys.argv) > 1:
+    REF = Path(sys.argv[1])
+elif os.environ.get("NANODRR_REFERENCE"):
+    REF = Path(os.environ["NANODRR_REFERENCE"])
+else:
+    sys.exit("usage: make_golden.py /path/to/nanodrr-checkout [case ...] (or set NANODRR_REFERENCE)")
 
 os.environ.setdefault("PYTHONDONTWRITEBYTECODE", "1")
 sys.dont_write_bytecode = True

@@ -200,3 +200,37 @@ def test_pose_entry_points_validate_on_the_host(lib):
     assert b(None, p, p, 4, p, p, p, 4, p, p, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
     assert b(p, p, p, 2, p, p, p, 4, p, p, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
     assert b(None, None, None, 1, None, None, None, 0, None, None, None) == _ffi.NDRR_OK
+
+
+@pytest.mark.parametrize("field,addr,expect", [
+    ("vol_quad", 0x7008, "vol_quad"),
+    ("gvol_quad", 0x7004, "gvol_quad"),
+    ("gvol", 0x9004, "gvol"),
+    ("M", 0x2002, "M"),
+    ("workspace", 0x6008, "workspace"),
+])
+def test_misaligned_pointers_are_refused_before_any_launch(lib, field, addr, expect):
+    """Pointers the kernels access with 16-byte vector instructions (quad
+    layout, its gradient scratch, the volume gradient the quad fold writes,
+    the workspace) and every element pointer must be aligned; a C caller
+    passing an offset view gets NDRR_ERR_INVALID_ARGUMENT, not a GPU fault."""
+    a = _valid_args()
+    a.vol_quad = 0x7000
+    a.go, a.go_dtype, a.gM = 0x4000, _ffi.NDRR_F32, 0x5000
+    a.need_gvol, a.gvol, a.gvol_quad = 1, 0x9000, 0x7000
+    a.workspace, a.workspace_bytes = 0x6000, 1 << 30
+    setattr(a, field, addr)
+    assert lib.ndrr_raymarch_bwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    msg = lib.ndrr_last_error().decode()
+    assert expect in msg and "aligned" in msg
+    nbytes = ctypes.c_uint64(0)
+    assert lib.ndrr_raymarch_bwd_workspace_bytes(ctypes.byref(a), ctypes.byref(nbytes)) == \
+        _ffi.NDRR_ERR_INVALID_ARGUMENT
+
+
+def test_quad_build_and_hu_to_mu_validate_on_the_host(lib):
+    assert lib.ndrr_quad_build(0x1000, _ffi.NDRR_F32, 4, 4, 4, 0x2008, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert lib.ndrr_hu_to_mu(0x1000, _ffi.NDRR_F32, -1, 0.02, 0.05, 1000.0, 0x1000, None) == \
+        _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert lib.ndrr_hu_to_mu(0x1000, _ffi.NDRR_U8, 4, 0.02, 0.05, 1000.0, 0x1000, None) == _ffi.NDRR_ERR_DTYPE
+    assert lib.ndrr_hu_to_mu(None, _ffi.NDRR_F32, 0, 0.02, 0.05, 1000.0, None, None) == _ffi.NDRR_OK

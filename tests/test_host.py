@@ -114,6 +114,72 @@ def test_subject_mu_cache_and_grid_affine():
         nd.Subject(hu, hu, eye, eye, eye, torch.zeros(3), bogus=1)
 
 
+def test_subject_mu_follows_settings_and_hu_tensor():
+    """The μ volume is rebuilt after a setting changes, after an in-place
+    edit of the HU values, after a new HU tensor is assigned and after a
+    dtype move; set_mu's result sticks until one of those happens."""
+    hu = torch.tensor([-500.0, 0.0, 250.0, 800.0]).reshape(1, 1, 1, 1, 4)
+    eye = torch.eye(4)
+    s = nd.Subject(hu.clone(), torch.zeros_like(hu), eye, eye, eye, torch.zeros(3))
+    first = s.image
+    assert s.image is first  # reused
+    s.hu_bone = 2000.0
+    assert s.image is not first
+    torch.testing.assert_close(s.image, nd.hu_to_mu(hu, hu_bone=2000.0))
+    before = s.image
+    s._image_hu.mul_(0.5)  # in-place edit of the HU values
+    torch.testing.assert_close(s.image, nd.hu_to_mu(hu * 0.5, hu_bone=2000.0))
+    assert s.image is not before
+    s._image_hu = hu.clone() + 100.0  # a new HU tensor
+    torch.testing.assert_close(s.image, nd.hu_to_mu(hu + 100.0, hu_bone=2000.0))
+    w = torch.tensor(0.03, requires_grad=True)
+    s.set_mu(mu_water=w)  # differentiable setting, stored settings unchanged
+    assert s.mu_water == nd.subject.MU_WATER
+    s.image.sum().backward()
+    assert w.grad is not None and w.grad.item() != 0.0
+    s.mu_bone = 0.06  # a setting change drops set_mu's result
+    torch.testing.assert_close(s.image, nd.hu_to_mu(hu + 100.0, mu_bone=0.06, hu_bone=2000.0))
+    s64 = s.double()
+    assert s64.image.dtype == torch.float64
+    s.convert_to_mu = False
+    assert s.image is s._image_hu
+    assert set(s.state_dict()) == {"_image_hu", "label", "voxel_to_world", "world_to_voxel", "voxel_to_grid",
+                                   "world_to_grid", "isocenter"}
+
+
+def test_hu_to_mu_piecewise_map_in_float64():
+    hu = torch.tensor([float("nan"), -3000.0, -1000.0, -250.0, 0.0, 1e-3, 600.0, 4000.0], dtype=torch.float64)
+    mu = nd.hu_to_mu(hu, 0.02, 0.05, 1500.0)
+    h = hu.clamp(min=-1000.0)
+    expect = torch.where(h <= 0, 0.02 * (1 + h / 1000), 0.02 + h / 1500.0 * 0.03).clamp(min=0.0)
+    torch.testing.assert_close(mu, expect, equal_nan=True)
+    assert torch.isnan(mu[0])
+
+
+def test_drr_rays_follow_the_intrinsics():
+    """DRR's src/tgt match the render call's ray construction and are rebuilt
+    when an intrinsic is reassigned or edited in place; state dict holds the
+    intrinsics only."""
+    drr = nd.DRR.from_carm_intrinsics(1020.0, 1.4, 1.4, 0.0, 0.0, 6, 5)
+    tgt = _make_tgt(drr.k_inv, drr.sdd, 6, 5, torch.device("cpu"), torch.float32)
+    torch.testing.assert_close(drr.tgt, tgt)
+    torch.testing.assert_close(drr.src, torch.zeros(1, 1, 3))
+    assert drr.tgt is drr.tgt  # kept while nothing changed
+    drr.sdd.mul_(0.5)
+    torch.testing.assert_close(drr.tgt, _make_tgt(drr.k_inv, drr.sdd, 6, 5, torch.device("cpu"), torch.float32))
+    drr.height = 3
+    assert drr.tgt.shape == (1, 15, 3)
+    drr.orthographic = True
+    torch.testing.assert_close(drr.src, _make_src(True, drr.tgt, drr.sdd))
+    drr.k_inv = drr.k_inv * 2.0
+    torch.testing.assert_close(drr.tgt, _make_tgt(drr.k_inv, drr.sdd, 3, 5, torch.device("cpu"), torch.float32))
+    assert set(drr.state_dict()) == {"k_inv", "sdd"}
+    k = drr.k_inv.clone().requires_grad_(True)
+    drr.k_inv = k
+    assert drr.tgt is not drr.tgt and drr.tgt.grad_fn is not None  # a fresh graph per read
+    assert drr.double().tgt.dtype == torch.float64
+
+
 def test_from_volume_centres_the_volume():
     s = nd.Subject.from_volume(torch.zeros(4, 6, 8), spacing=(0.5, 1.0, 2.0))
     c = s.voxel_to_world @ torch.tensor([3.5, 2.5, 1.5, 1.0])

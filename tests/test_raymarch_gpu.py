@@ -504,6 +504,9 @@ def test_tma_staged_forward_variant_is_bitwise_the_default(seed, vol_shape):
     out, _ = raymarch_forward(v, v, t(M), t(src), t(tgt), t(step), n, 1, width, fwd_mode=1)
     assert torch.isfinite(out).all()
     assert torch.equal(out, ref)
+    from nanodrr_gb300.raymarch import device_flags
+
+    assert device_flags() & _ffi.NDRR_FLAG_TMA_TIMEOUT == 0  # no stage wait gave up
 
 
 def test_rays_that_miss_the_volume_on_every_path():

@@ -148,6 +148,10 @@ def test_graphed_step_replays_the_eager_step():
     assert torch.equal(loss_3, ref3[0])
     assert torch.equal(step.grads[0], ref3[1]) and torch.equal(step.grads[1], ref3[2])
     assert not torch.equal(ref2[0], ref3[0])
+    # a different volume tensor cannot be followed by the graph: replay refuses
+    sub._image_hu = vol.detach().clone().requires_grad_(True)
+    with pytest.raises(RuntimeError, match="captured"):
+        step.replay()
 
 
 def _torch_pose64(rot, xyz, rt, piv, piv_inv):
