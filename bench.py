@@ -26,6 +26,7 @@ from __future__ import annotations
 import argparse
 import json
 import os
+import shutil
 import statistics
 import subprocess
 import sys
@@ -40,9 +41,12 @@ import torch  # noqa: E402
 
 BASELINE_HEADLINE = None  # no published number exists for this metric
 METRIC = "fwd+bwd DRR frames/s at 512^3/256^2, learned-skip vs plain kernel"
-# DRAM read + write bytes per sample of the slab-ordered adjoint kernel from
-# an ncu capture (profiles/raymarch_bwd_slab_kernel_quad_gvol_f32_384cube_8poses.md)
+# DRAM read + write bytes per sample of the slab-ordered adjoint kernel,
+# measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum of one launch)
+# on a 384^3 x 8-pose case of the same kernel and scaled here by the samples
+# of a launch.
 SLAB_DRAM_BYTES_PER_SAMPLE = 25.16
+SLAB_DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, 384^3 x 8 poses, scaled per sample"
 
 
 def parse_args():
@@ -65,6 +69,8 @@ def parse_args():
     p.add_argument("--no-batched", action="store_true", help="skip the uneven batched-launch measurement")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the per-label forward and the 1024^2 learned-proposal measurements")
+    p.add_argument("--no-reference-kernel", action="store_true",
+                   help="skip timing the reference's Triton kernel from baseline/_ref")
     p.add_argument("--no-graph", action="store_true",
                    help="time eager steps only (no CUDA-graph capture; for profilers that cannot follow a capture)")
     return p.parse_args()
@@ -362,6 +368,12 @@ def run_ours(args, world, rank, local):
         gvol = torch.zeros_like(vol)
         quad = cached_quad(sub, vol)
         reps = max(3, args.steps)
+        bwd_kernel_ms = _kernel_only_ms(
+            lambda: raymarch_backward(go, vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, True, False, gvol=gvol,
+                                      quad=quad), reps)
+        fwd_kernel_ms = _kernel_only_ms(lambda: raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd,
+                                                                 quad=quad), reps)
+        l2 = l2_read_peak(dev)
         times = {"fwd": [], "fwd_learned": [], "bwd": [], "fwd_plain_layout": [], "bwd_plain_layout": [],
                  "learned_windows": [], "bwd_direct": []}
         for i in range(reps + 1):
@@ -398,32 +410,44 @@ def run_ours(args, world, rank, local):
     fwd_s = statistics.median(times["fwd"]) / 1e3
     bwd_s = statistics.median(times["bwd"]) / 1e3
     fwdl_s = statistics.median(times["fwd_learned"]) / 1e3
+    kern_s = bwd_kernel_ms / 1e3
     peaks = _peaks()
-    achieved = bwd_bytes / bwd_s / 1e9
+    traffic = SLAB_DRAM_BYTES_PER_SAMPLE * n_samp
+    dram_gbs = traffic / kern_s / 1e9
+    demand_gbs = bwd_bytes / kern_s / 1e9
     st = stats.tolist()
     ost = occ_stats.tolist()
     roofline = {
         "bound": "hbm",
         "kernel": "raymarch_bwd_slab_kernel (adjoint with pose and volume gradient, slab-ordered, quad layout)",
-        "timed": "the whole adjoint call on its stream: gradient memset, slab plan, kernel, pose reduction, fold",
-        "achieved": round(achieved, 1),
+        "timed": "the march kernel alone (CUDA events the library records around it on the launch stream)",
+        # DRAM bytes of one launch per kernel time, against the measured HBM
+        # copy bandwidth: the fraction of HBM the kernel uses
+        "achieved": round(dram_gbs, 1),
         "peak": peaks["hbm_gbs"],
         "peak_source": peaks["source"],
         "unit": "GB/s",
-        "frac": round(achieved / peaks["hbm_gbs"], 4),
-        # DRAM bytes of the kernel per sample from the ncu capture of the
-        # 384^3 x 8-pose case, scaled by this launch's samples
-        "traffic": round(SLAB_DRAM_BYTES_PER_SAMPLE * n_samp, 1) if SLAB_DRAM_BYTES_PER_SAMPLE else None,
-        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, 384^3 x 8 poses, scaled per sample",
+        "frac": round(dram_gbs / peaks["hbm_gbs"], 4),
+        "traffic": round(traffic, 1),
+        "traffic_source": SLAB_DRAM_SOURCE,
+        # the per-sample demand bytes (8 corner reads, the upstream gradient,
+        # 8 corner read-modify-writes), mostly served by L1 and L2, against the
+        # L2 read bandwidth measured by the library's probe in this run
         "algorithmic_bytes_per_launch": bwd_bytes,
+        "demand_gbs": round(demand_gbs, 1),
+        "l2_peak_gbs": l2["gbs"],
+        "l2_peak_how": l2["how"],
+        "l2_frac": round(demand_gbs / l2["gbs"], 4) if l2["gbs"] else None,
         "samples_per_launch": n_samp,
+        "kernel_ms": round(bwd_kernel_ms, 3),
+        "call_ms": round(bwd_s * 1e3, 3),
+        "fwd_kernel_ms": round(fwd_kernel_ms, 3),
         "fwd_ms": round(fwd_s * 1e3, 3),
         "fwd_learned_ms": round(fwdl_s * 1e3, 3),
         "learned_windows_ms": round(statistics.median(times["learned_windows"]), 3),
-        "bwd_ms": round(bwd_s * 1e3, 3),
         "fwd_gsamples_per_s": round(n_samp / fwd_s / 1e9, 2),
-        "bwd_gsamples_per_s": round(n_samp / bwd_s / 1e9, 2),
-        "fwd_frac_of_hbm": round(fwd_bytes / fwd_s / 1e9 / peaks["hbm_gbs"], 4),
+        "bwd_gsamples_per_s": round(n_samp / kern_s / 1e9, 2),
+        "fwd_demand_l2_frac": round(fwd_bytes / (fwd_kernel_ms / 1e3) / 1e9 / l2["gbs"], 4) if l2["gbs"] else None,
         "plain_layout_fwd_ms": round(statistics.median(times["fwd_plain_layout"]), 3),
         "plain_layout_bwd_ms": round(statistics.median(times["bwd_plain_layout"]), 3),
         "direct_scatter_bwd_ms": round(statistics.median(times["bwd_direct"]), 3),
@@ -449,9 +473,20 @@ def run_ours(args, world, rank, local):
             "bitwise_equal_to_software": bool(torch.equal(tma, plain16)),
         }
         del soft, hard, tma, plain16
-    cpu = None
+    ref_kernel = None
+    if rank == 0 and not args.no_reference_kernel:
+        torch.cuda.empty_cache()
+        try:
+            ref_kernel = reference_triton(args, dev, sub, k_inv, sdd, rt, target, args.steps)
+        except Exception as e:  # the reference's kernel failing must not lose this run's line
+            ref_kernel = {"unavailable": f"the reference's Triton path raised {type(e).__name__}: {e}"[:300]}
+    cpu = parity = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, sub, k_inv, sdd, rt)
+        try:
+            parity = parity_vs_oracle(args, sub, k_inv, sdd, rt, skips)
+        except Exception as e:
+            parity = {"error": f"{type(e).__name__}: {e}"[:300]}
     uneven = labels = leval = sparse = single = None
     if not args.no_batched:
         del reg, skips
@@ -465,7 +500,7 @@ def run_ours(args, world, rank, local):
         torch.cuda.empty_cache()
         sparse = sparse_phantom_skip(dev)
         torch.cuda.empty_cache()
-        single = single_frame_forward(dev)
+        single = single_frame_forward(dev, with_reference=not args.no_reference_kernel)
     out = {
         "metric": METRIC,
         "value": round(value, 2),
@@ -518,6 +553,12 @@ def run_ours(args, world, rank, local):
     }
     if cpu is not None:
         out["cpu_baseline"] = cpu
+    if parity is not None:
+        out["parity"] = parity
+    if ref_kernel is not None:
+        out["reference_triton"] = ref_kernel
+        if "frames_per_s" in ref_kernel:
+            out["vs_reference_triton"] = round(value / ref_kernel["frames_per_s"], 2)
     if uneven is not None:
         out["batched_uneven"] = uneven
     if labels is not None:
@@ -632,6 +673,67 @@ def _event_ms(fn, steps):
     return statistics.median(ts)
 
 
+def _kernel_only_ms(fn, reps):
+    """Median duration (ms) of the ray-march kernel inside `fn`: the library
+    records a pair of CUDA events on the launch stream just before and after
+    its march kernel (ndrr_set_kernel_events), so the call's other launches
+    (gradient zeroing, slab planning, pose reduction, fold) are excluded."""
+    import ctypes
+
+    from nanodrr_gb300 import _ffi
+
+    lib = _ffi.load()
+    fn()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        e1.record()  # creates both events before the library records them
+        torch.cuda.synchronize()
+        _ffi.check(lib.ndrr_set_kernel_events(ctypes.c_void_p(e0.cuda_event), ctypes.c_void_p(e1.cuda_event)),
+                   "ndrr_set_kernel_events")
+        try:
+            fn()
+        finally:
+            lib.ndrr_set_kernel_events(None, None)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return statistics.median(ts)
+
+
+def l2_read_peak(dev, mib=32, passes=64, reps=7):
+    """Measured L2 read bandwidth (GB/s): the library's probe streams an
+    L2-resident buffer `passes` times with L2-only loads; best of `reps`,
+    CUDA events around each launch."""
+    import ctypes
+
+    from nanodrr_gb300 import _ffi
+
+    lib = _ffi.load()
+    buf = torch.zeros(mib << 20, dtype=torch.uint8, device=dev)
+    sink = torch.zeros(1, dtype=torch.int32, device=dev)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+
+    def launch():
+        _ffi.check(lib.ndrr_l2_read_probe(ctypes.c_void_p(buf.data_ptr()), ctypes.c_uint64(buf.numel()), passes,
+                                          ctypes.c_void_p(sink.data_ptr()), ctypes.c_void_p(stream)),
+                   "ndrr_l2_read_probe")
+
+    launch()
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        launch()
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, buf.numel() * passes / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    return {"gbs": round(best, 1), "how": f"{mib} MiB buffer read {passes}x with ld.global.cg by 4 CTAs x 512 "
+            f"threads per SM, best of {reps}, CUDA events"}
+
+
 def _rays(sub, rt, k_inv, sdd, det, S):
     from nanodrr_gb300.renderer import _affine_product, _make_src, _make_tgt
 
@@ -645,7 +747,8 @@ def _rays(sub, rt, k_inv, sdd, det, S):
 
 def _rel_maxabs(a, b):
     """max over images of max|a - b| / max|b| (images = leading dims but the last)."""
-    a, b = a.float().flatten(0, -2), b.float().flatten(0, -2)
+    a, b = a.double().flatten(0, -2), b.double().flatten(0, -2)
+    b = b.to(a.device)
     num = (a - b).abs().amax(-1)
     den = b.abs().amax(-1).clamp_min(1e-30)
     return float((num / den).max())
@@ -697,7 +800,7 @@ def _skip_kwargs(es, vol, M, src, tgt, step, S, det):
     return {"skip": es}
 
 
-def single_frame_forward(dev, runs=10, iters=100, warmup=25):
+def single_frame_forward(dev, runs=10, iters=100, warmup=25, with_reference=True):
     """The shape of the reference's published benchmark (tests/benchmark/
     benchmark.py:23-47, 58-96): one AP pose 850 mm from the isocenter, 200^2
     detector at 2.0 mm, sdd 1020, 500 samples, fp32 forward, on the 512 x 512
@@ -743,9 +846,145 @@ def single_frame_forward(dev, runs=10, iters=100, warmup=25):
         with torch.cuda.graph(graph):
             call()
         graphed = wall_us(graph.replay)
-    return {"workload": "1 AP pose, 200^2 detector at 2.0 mm, 500 samples, fp32 forward, 512x512x400 phantom",
-            "render_call_us": round(eager, 1), "render_call_frames_per_s": round(1e6 / eager, 1),
-            "graph_replay_us": round(graphed, 1), "graph_replay_frames_per_s": round(1e6 / graphed, 1)}
+        res = {"workload": "1 AP pose, 200^2 detector at 2.0 mm, 500 samples, fp32 forward, 512x512x400 phantom",
+               "render_call_us": round(eager, 1), "render_call_frames_per_s": round(1e6 / eager, 1),
+               "graph_replay_us": round(graphed, 1), "graph_replay_frames_per_s": round(1e6 / graphed, 1)}
+        # the reference's own Triton kernel, the same call timed the same way
+        ref, why = load_reference() if with_reference else (None, "not requested")
+        if ref is None:
+            res["reference_triton"] = {"unavailable": why}
+        else:
+            rsub = reference_subject(ref, sub._image_hu, sub.world_to_voxel, sub.voxel_to_world, sub.isocenter)
+            rcall = lambda: ref["render"](rsub, k_inv, rt, sdd, 200, 200, n_samples=500, backend="triton")  # noqa: E731
+            r_us = wall_us(rcall)
+            res["reference_triton"] = {"render_call_us": round(r_us, 1), "render_call_frames_per_s": round(1e6 / r_us, 1),
+                                       "image_rel_maxabs_vs_this_library": round(_rel_maxabs(call(), rcall()), 8)}
+    return res
+
+
+# ------------------------------------------------ the reference's own kernel
+REF_DIR = ROOT / "baseline" / "_ref"
+
+
+def load_reference():
+    """The unmodified reference package from baseline/_ref (installed by
+    baseline/install_reference.py) and its Triton backend, or a reason why it
+    cannot run here. Triton's bundled ptxas predates sm_103a, so the CUDA
+    toolkit's ptxas is named for it (TRITON_PTXAS_PATH) unless one is set."""
+    if not (REF_DIR / "nanodrr").is_dir():
+        return None, "baseline/_ref is not installed (python baseline/install_reference.py <nanodrr checkout>)"
+    if "TRITON_PTXAS_PATH" not in os.environ:
+        for cand in (shutil.which("ptxas"), "/usr/local/cuda/bin/ptxas"):
+            if cand and Path(cand).exists():
+                os.environ["TRITON_PTXAS_PATH"] = cand
+                break
+    try:
+        import triton  # noqa: F401
+    except Exception as e:  # pragma: no cover - depends on the host
+        return None, f"triton is not importable: {e}"
+    if str(REF_DIR) not in sys.path:
+        sys.path.insert(0, str(REF_DIR))
+    try:
+        from nanodrr.data import Subject as RefSubject
+        from nanodrr.drr.renderer import _triton_available
+        from nanodrr.drr.renderer import render as ref_render
+        from nanodrr.metrics import NormalizedCrossCorrelation2d as RefNCC
+    except Exception as e:
+        return None, f"the reference does not import: {e}"
+    if not _triton_available():
+        return None, "the reference's Triton backend does not import"
+    return {"Subject": RefSubject, "render": ref_render, "NCC": RefNCC}, None
+
+
+def reference_subject(ref, image, world_to_voxel, voxel_to_world, isocenter):
+    """The reference's Subject around a [1, 1, D, H, W] attenuation volume."""
+    return ref["Subject"](
+        imagedata=image,
+        labeldata=torch.zeros_like(image.detach()),
+        voxel_to_world=voxel_to_world,
+        world_to_voxel=world_to_voxel,
+        voxel_to_grid=ref["Subject"]._make_voxel_to_grid(image.shape).to(image.device),
+        isocenter=isocenter,
+        max_label=0,
+        convert_to_mu=False,
+    )
+
+
+def reference_triton(args, dev, sub, k_inv, sdd, rt, target, steps):
+    """The reference's fused Triton kernel on this GPU through its own
+    render(..., backend="triton") and NormalizedCrossCorrelation2d, on the
+    headline workload: fwd + NCC + bwd to the pose (its rt_inv; the se(3)
+    chain of its Registration module needs roma, which is not installed) and
+    to the volume, CUDA events around `steps` eager steps after the same
+    warm-up; plus the forward alone and parity of its image and gradients
+    with this library's on the same inputs."""
+    import nanodrr_gb300 as nd
+    from nanodrr_gb300.registration import NormalizedCrossCorrelation2d
+
+    ref, why = load_reference()
+    if ref is None:
+        return {"unavailable": why}
+    B, Hd, S = rt.shape[0], args.det, args.samples
+    vol_leaf = sub._image_hu.detach().clone().requires_grad_(True)
+    rsub = reference_subject(ref, vol_leaf, sub.world_to_voxel, sub.voxel_to_world, sub.isocenter)
+    rncc = ref["NCC"]()
+    rt_leaf = rt.detach().clone().requires_grad_(True)
+
+    def step():
+        vol_leaf.grad = None
+        rt_leaf.grad = None
+        img = ref["render"](rsub, k_inv, rt_leaf, sdd, Hd, Hd, n_samples=S, backend="triton")
+        loss = -rncc(img, target).mean()
+        loss.backward()
+        return loss
+
+    t0 = time.perf_counter()
+    step()
+    torch.cuda.synchronize()
+    compile_s = time.perf_counter() - t0
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        step()
+    e1.record()
+    torch.cuda.synchronize()
+    step_s = e0.elapsed_time(e1) / 1e3 / steps
+    with torch.no_grad():
+        fwd = lambda: ref["render"](rsub, k_inv, rt, sdd, Hd, Hd, n_samples=S, backend="triton")  # noqa: E731
+        fwd_ms = _event_ms(fwd, max(3, steps))
+        ref_img = fwd()
+    # the same step through this library (render + NCC kernels) for parity
+    step()
+    g_rt_ref, g_vol_ref = rt_leaf.grad.clone(), vol_leaf.grad.clone()
+    keep = sub._image_hu
+    mine_vol = sub._image_hu.detach().clone().requires_grad_(True)
+    sub._image_hu = mine_vol
+    try:
+        rt_mine = rt.detach().clone().requires_grad_(True)
+        img = nd.render(sub, k_inv, rt_mine, sdd, Hd, Hd, n_samples=S)
+        (-NormalizedCrossCorrelation2d()(img, target).mean()).backward()
+    finally:
+        sub._image_hu = keep
+    res = {
+        "impl": "reference render(..., backend='triton') from baseline/_ref, unmodified; TRITON_PTXAS_PATH = "
+                + os.environ.get("TRITON_PTXAS_PATH", "default"),
+        "frames_per_s": round(B / step_s, 2),
+        "ms_per_step": round(step_s * 1e3, 3),
+        "fwd_frames_per_s": round(B / fwd_ms * 1e3, 2),
+        "first_call_s": round(compile_s, 2),
+        "parity_vs_this_library": {
+            "image_rel_maxabs": round(_rel_maxabs(img.detach(), ref_img), 8),
+            "pose_grad_rel_maxabs": round(_rel_maxabs(rt_mine.grad[:, :3].reshape(1, -1),
+                                                      g_rt_ref[:, :3].reshape(1, -1)), 8),
+            "volume_grad_rel_maxabs": round(_rel_maxabs(mine_vol.grad.reshape(1, -1),
+                                                        g_vol_ref.reshape(1, -1)), 8),
+        },
+    }
+    del rsub, vol_leaf, mine_vol
+    return res
 
 
 def sparse_phantom_skip(dev, steps=5, epochs=40, body_scale=0.4, train_poses=64):
@@ -901,6 +1140,60 @@ def _cpu_sample(args, vol_cpu, w2v, k_inv, sdd, rt, rays):
     out = render_oracle(vol, None, w2v, rtp, src, tgt, args.samples, 1)
     out.sum().backward()
     return out
+
+
+def parity_vs_oracle(args, sub, k_inv, sdd, rt, skips, poses=2, rays=2048):
+    """FP64 parity of the headline workload, computed in the CPU-baseline leg
+    where the oracle is the checker: a seeded subset of `rays` pixels of each
+    of the first `poses` poses is rendered by the CUDA path (plain march and
+    learned proposal) with gradients to rt_inv and to the volume of a
+    positively weighted ray sum, and by the float64 restatement of the
+    reference's PyTorch backend on the host from the same float32 inputs;
+    relative max-abs errors (image per pose, gradients overall)."""
+    import nanodrr_gb300 as nd
+    from nanodrr_gb300.renderer import _make_tgt
+    from oracle import render_oracle
+
+    dev = rt.device
+    Hd, S = args.det, args.samples
+    g = torch.Generator().manual_seed(11)
+    idx = torch.stack([torch.randperm(Hd * Hd, generator=g)[:rays] for _ in range(poses)])
+    tgt = _make_tgt(k_inv, sdd, Hd, Hd, dev, torch.float32)[0][idx.to(dev)].contiguous()
+    src = torch.zeros(poses, 1, 3, device=dev)
+    tgt64 = _make_tgt(k_inv.double().cpu(), sdd.double().cpu(), Hd, Hd, "cpu", torch.float64)[0][idx]
+    src64 = torch.zeros(poses, 1, 3, dtype=torch.float64)
+    weight = 0.5 + torch.rand(poses, 1, rays, generator=g, dtype=torch.float64)
+    vol64 = sub._image_hu.detach()[0, 0].double().cpu().requires_grad_(True)
+    w2v64 = sub.world_to_voxel.double().cpu()
+    rt64 = rt[:poses].detach().double().cpu().requires_grad_(True)
+    ref = render_oracle(vol64, None, w2v64, rt64, src64, tgt64, S)
+    (ref * weight).sum().backward()
+    ref = ref.detach()
+    res = {"oracle": "float64 restatement of the reference's PyTorch backend on the host, same float32 inputs",
+           "rays": f"{rays} seeded pixels of each of the first {poses} poses, {S} samples",
+           "tolerances": {"image": 1e-5, "gradients": 1e-3}}
+    keep = sub._image_hu
+    w = weight.float().to(dev)
+    for name in ("plain", "learned"):
+        vol = keep.detach().clone().requires_grad_(True)
+        sub._image_hu = vol
+        sub.empty_space = skips[name]
+        try:
+            rtp = rt[:poses].detach().clone().requires_grad_(True)
+            out = nd.render(sub, k_inv, rtp, sdd, rays // 64, 64, n_samples=S, src=src, tgt=tgt)
+            out = out.reshape(poses, 1, rays)
+            (out * w).sum().backward()
+        finally:
+            sub._image_hu = keep
+            sub.empty_space = None
+        res[name] = {
+            "image_rel_maxabs": _rel_maxabs(out.detach().double().cpu()[:, 0], ref[:, 0]),
+            "pose_grad_rel_maxabs": _rel_maxabs(rtp.grad[:, :3].reshape(1, -1).double().cpu(),
+                                                rt64.grad[:, :3].reshape(1, -1)),
+            "volume_grad_rel_maxabs": _rel_maxabs(vol.grad.reshape(1, -1).double().cpu(),
+                                                  vol64.grad.reshape(1, -1)),
+        }
+    return res
 
 
 def cpu_baseline(args, sub, k_inv, sdd, rt):

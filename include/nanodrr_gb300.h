@@ -182,7 +182,8 @@ typedef struct ndrr_raymarch_args {
     /* Launch tuning; 0 selects the library default for each. */
     int32_t tile_w;         /* detector tile width in rays (8 or 16)            */
     int32_t tile_h;         /* detector tile height in rays (8 or 16)           */
-    int32_t sample_split;   /* 1, 2 or 4 sample chunks per ray within a CTA     */
+    int32_t sample_split;   /* 1, 2, 4, 8 or 16 sample chunks per ray within a
+                               CTA (tile_w * tile_h * sample_split <= 512)      */
     int32_t gvol_mode;      /* adjoint volume-gradient scatter: 0 auto,
                                1 direct global atomics per tap, 2 per-slab
                                shared-memory brick flushed with coalesced
@@ -234,6 +235,10 @@ enum ndrr_gvol_mode {
     NDRR_GVOL_DIRECT = 1,
     NDRR_GVOL_BRICK = 2,
     NDRR_GVOL_SLAB = 3,
+    NDRR_GVOL_SLAB_WARP = 4, /* NDRR_GVOL_SLAB with warp aggregation: lanes of a
+                                warp scattering into the same quad cell in the
+                                same step combine their terms before the
+                                reduction (__match_any_sync + shuffles)      */
 };
 
 /* Library identity. */
@@ -452,6 +457,23 @@ NDRR_API int32_t ndrr_quad_build(const void* vol, int32_t vol_dtype, int32_t D, 
  * 0. Computed in fp32. */
 NDRR_API int32_t ndrr_hu_to_mu(const void* hu, int32_t dtype, int64_t n, float mu_water, float mu_bone,
                                float hu_bone, void* mu, void* stream);
+
+/* ---- measurement ------------------------------------------------------------ *
+ * Kernel timing hook: while set, the calling thread's ray-march entry points
+ * record `start` (a cudaEvent_t) on their stream just before each ray-march
+ * kernel they launch and `stop` just after it, so cudaEventElapsedTime gives
+ * the march kernel's own duration apart from the other launches of the same
+ * call (gradient zeroing, slab planning, pose reduction, gradient fold).
+ * ndrr_set_kernel_events(NULL, NULL) turns it off. With more than one march
+ * kernel per call the events bracket the last one. */
+NDRR_API int32_t ndrr_set_kernel_events(void* start, void* stop);
+
+/* L2 read-bandwidth probe: streams `bytes` of `buf` (device, 16-byte
+ * aligned, contents arbitrary) `passes` times with L2-only loads from 4 CTAs
+ * of 512 threads per SM; time it with events around the call. A buffer well
+ * below the L2 size is read from L2 after the first pass. `sink` (device, 4
+ * bytes) is written only in a case real data does not reach. */
+NDRR_API int32_t ndrr_l2_read_probe(const void* buf, uint64_t bytes, int32_t passes, uint32_t* sink, void* stream);
 
 /* ---- empty-space structures ---------------------------------------------- */
 typedef struct ndrr_occupancy_args {

@@ -29,7 +29,7 @@ NDRR_F32, NDRR_F16, NDRR_BF16, NDRR_U8, NDRR_I8, NDRR_I16, NDRR_I32, NDRR_I64 = 
 ABI_VERSION = 2
 
 # ndrr_gvol_mode
-NDRR_GVOL_AUTO, NDRR_GVOL_DIRECT, NDRR_GVOL_BRICK = 0, 1, 2
+NDRR_GVOL_AUTO, NDRR_GVOL_DIRECT, NDRR_GVOL_BRICK, NDRR_GVOL_SLAB, NDRR_GVOL_SLAB_WARP = 0, 1, 2, 3, 4
 
 _c_float_p = ctypes.POINTER(ctypes.c_float)
 
@@ -151,6 +151,9 @@ SIGNATURES: dict[str, tuple] = {
     "ndrr_quad_build": (ctypes.c_int32, [ctypes.c_void_p] + [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 2),
     "ndrr_hu_to_mu": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
                                        ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]),
+    "ndrr_set_kernel_events": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p]),
+    "ndrr_l2_read_probe": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p,
+                                            ctypes.c_void_p]),
     "ndrr_occupancy_dims": (ctypes.c_int32, [ctypes.c_int32] * 4 + [_i32p] * 3),
     "ndrr_occupancy_build": (ctypes.c_int32, [ctypes.POINTER(OccupancyArgs), ctypes.c_void_p]),
     "ndrr_skip_windows": (ctypes.c_int32, [ctypes.POINTER(RaymarchArgs), ctypes.c_void_p, ctypes.c_void_p]),

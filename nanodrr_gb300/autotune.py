@@ -23,7 +23,8 @@ from .raymarch import raymarch_backward, raymarch_forward
 # (tile_w, tile_h, sample_split) with 256 threads: the batched kernel's shapes.
 BATCHED_CANDIDATES = [(16, 16, 1), (16, 8, 2), (8, 8, 4), (32, 8, 1)]
 # shapes for the single-request kernels (up to 512 threads)
-SINGLE_CANDIDATES = [(16, 8, 1), (16, 16, 1), (32, 8, 1), (16, 8, 2), (8, 8, 4), (16, 8, 4)]
+SINGLE_CANDIDATES = [(16, 8, 1), (16, 16, 1), (32, 8, 1), (16, 8, 2), (8, 8, 4), (16, 8, 4), (8, 4, 4), (8, 4, 8),
+                     (8, 8, 8), (8, 4, 16)]
 # quad-gradient MiB per slab for the slab-ordered volume-gradient adjoint
 SLAB_CANDIDATES = [48, 96, 192]
 

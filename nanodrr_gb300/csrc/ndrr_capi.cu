@@ -134,8 +134,9 @@ int32_t validate_common(const ndrr_raymarch_args* a) {
         return fail(NDRR_ERR_INVALID_ARGUMENT, "tile_w must be a multiple of 8 in [8, 64] (got %d)", a->tile_w);
     if (a->tile_h != 0 && (a->tile_h % 4 != 0 || a->tile_h < 4 || a->tile_h > 64))
         return fail(NDRR_ERR_INVALID_ARGUMENT, "tile_h must be a multiple of 4 in [4, 64] (got %d)", a->tile_h);
-    if (a->sample_split != 0 && a->sample_split != 1 && a->sample_split != 2 && a->sample_split != 4)
-        return fail(NDRR_ERR_INVALID_ARGUMENT, "sample_split must be 1, 2 or 4 (got %d)", a->sample_split);
+    if (a->sample_split != 0 && a->sample_split != 1 && a->sample_split != 2 && a->sample_split != 4 &&
+        a->sample_split != 8 && a->sample_split != 16)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "sample_split must be 1, 2, 4, 8 or 16 (got %d)", a->sample_split);
     if (a->skip_mode < NDRR_SKIP_NONE || a->skip_mode > NDRR_SKIP_PROPOSAL)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "skip_mode must be 0, 1 or 2 (got %d)", a->skip_mode);
     if (a->skip_mode != NDRR_SKIP_NONE) {
@@ -159,10 +160,10 @@ int32_t validate_common(const ndrr_raymarch_args* a) {
         return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_overwrite is 0, or 1 with the quad layout");
     if (a->fwd_mode != NDRR_FWD_DEFAULT && a->fwd_mode != NDRR_FWD_TMA)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "fwd_mode must be 0 or 1 (got %d)", a->fwd_mode);
-    if (a->gvol_mode < NDRR_GVOL_AUTO || a->gvol_mode > NDRR_GVOL_SLAB)
-        return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode must be 0, 1, 2 or 3 (got %d)", a->gvol_mode);
-    if (a->gvol_mode == NDRR_GVOL_SLAB && a->vol_quad == nullptr)
-        return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode 3 (slab-ordered) needs the quad layout (vol_quad)");
+    if (a->gvol_mode < NDRR_GVOL_AUTO || a->gvol_mode > NDRR_GVOL_SLAB_WARP)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode must be 0 .. 4 (got %d)", a->gvol_mode);
+    if ((a->gvol_mode == NDRR_GVOL_SLAB || a->gvol_mode == NDRR_GVOL_SLAB_WARP) && a->vol_quad == nullptr)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode 3 and 4 (slab-ordered) need the quad layout (vol_quad)");
     if (a->brick_cap < 0 || a->brick_cap > 56 * 1024)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "brick capacity %d out of range [0, 57344] voxels", a->brick_cap);
     if (a->slab_mib < 0 || a->slab_mib > 4096)
@@ -497,6 +498,25 @@ int32_t ndrr_hu_to_mu(const void* hu, int32_t dtype, int64_t n, float mu_water, 
     const cudaError_t e =
         ndrr::launch_hu_to_mu(hu, dtype, n, mu_water, dmu, hu_bone, mu, reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "HU conversion launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
+int32_t ndrr_set_kernel_events(void* start, void* stop) {
+    if ((start == nullptr) != (stop == nullptr))
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "start and stop events are both set or both NULL");
+    ndrr::KernelEvents& ev = ndrr::kernel_events();
+    ev.start = reinterpret_cast<cudaEvent_t>(start);
+    ev.stop = reinterpret_cast<cudaEvent_t>(stop);
+    return ok();
+}
+
+int32_t ndrr_l2_read_probe(const void* buf, uint64_t bytes, int32_t passes, uint32_t* sink, void* stream) {
+    if (buf == nullptr || sink == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "buf and sink must be non-NULL");
+    if (misaligned(buf, 16) || bytes < 16 || passes < 1)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "the probe needs a 16-byte aligned buffer of >= 16 bytes, passes >= 1");
+    const cudaError_t e = ndrr::launch_l2_probe(buf, bytes, passes, sink, sm_count_current(),
+                                                reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "probe launch failed: %s", cudaGetErrorString(e));
     return ok();
 }
 

@@ -19,6 +19,17 @@ struct LaunchShape {
     bool slab = false;   // adjoint with volume gradient ordered slab by slab (quad layout)
 };
 
+// Measurement hook (ndrr_set_kernel_events): CUDA events recorded on the
+// launch stream just before and just after each ray-march kernel launch of
+// the calling thread; NULL when off.
+struct KernelEvents {
+    cudaEvent_t start = nullptr;
+    cudaEvent_t stop = nullptr;
+};
+KernelEvents& kernel_events();
+cudaError_t launch_l2_probe(const void* buf, unsigned long long bytes, int passes, unsigned* sink, int sm_count,
+                            cudaStream_t st);
+
 LaunchShape choose_shape(const ndrr_raymarch_args& a, int sm_count);
 uint64_t bwd_workspace_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
 size_t fwd_smem_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);

@@ -57,8 +57,18 @@ MarchParams make_params(const ndrr_raymarch_args& a, const LaunchShape& ls) {
 LaunchShape choose_shape(const ndrr_raymarch_args& a, int sm_count) {
     LaunchShape ls;
     ls.sm = sm_count;
-    ls.tw = a.tile_w > 0 ? a.tile_w : 16;
-    ls.th = a.tile_h > 0 ? a.tile_h : 8;
+    // A small launch (fewer than kSmallLaunchRays rays, e.g. one frame of a
+    // 200^2 detector = 40 000 rays) takes narrow 8 x 4-ray tiles unless the
+    // caller chose a tile: with 16 x 8 tiles split 4 ways one such frame was
+    // 325 CTAs of 512 threads, at most two resident per SM, so 21 CTAs ran as
+    // a second wave as long as the first; 8 x 4 tiles give 1250 CTAs of 128
+    // threads, all resident at once. The rule depends on the ray count only,
+    // never on the device, because the adjoint's workspace size (partials per
+    // tile) is computed without a device query and must match the launch.
+    constexpr double kSmallLaunchRays = 65536.0;
+    const bool small = (double)a.B * a.N < kSmallLaunchRays && a.tile_w == 0 && a.tile_h == 0;
+    ls.tw = a.tile_w > 0 ? a.tile_w : (small ? 8 : 16);
+    ls.th = a.tile_h > 0 ? a.tile_h : (small ? 4 : 8);
     const TileMap tm = make_tilemap(a.N, a.width, ls.tw, ls.th);
     const double threads = (double)a.B * tm.tiles * ls.tw * ls.th;
     const double want = (double)sm_count * 1024.0;
@@ -66,8 +76,10 @@ LaunchShape choose_shape(const ndrr_raymarch_args& a, int sm_count) {
         ls.K = a.sample_split;
     } else {
         // Split each ray's samples across threads only when the rays alone
-        // leave the GPU under-filled (about 1024 resident threads per SM).
-        ls.K = threads >= want ? 1 : (threads * 2 >= want ? 2 : 4);
+        // leave the GPU under-filled (about 1024 resident threads per SM):
+        // the smallest power of two up to 16 that reaches it.
+        ls.K = 1;
+        while (ls.K < 16 && threads * ls.K < want) ls.K *= 2;
         if (ls.tw * ls.th * ls.K > 512) ls.K = std::max(1, 512 / (ls.tw * ls.th));
     }
     // Volume-gradient scatter: direct global atomics by default; they
@@ -80,8 +92,8 @@ LaunchShape choose_shape(const ndrr_raymarch_args& a, int sm_count) {
     // Slab-ordered volume-gradient adjoint (the default for the quad layout
     // without camera gradients; measured 11 % faster than direct scatter at
     // 512^3 x 32 poses).
-    ls.slab = (a.gvol_mode == NDRR_GVOL_SLAB || a.gvol_mode == NDRR_GVOL_AUTO) && a.vol_quad != nullptr &&
-              a.need_gvol && !a.need_gcam;
+    ls.slab = (a.gvol_mode == NDRR_GVOL_SLAB || a.gvol_mode == NDRR_GVOL_SLAB_WARP ||
+               a.gvol_mode == NDRR_GVOL_AUTO) && a.vol_quad != nullptr && a.need_gvol && !a.need_gcam;
     if (ls.brick) {
         ls.K = 1;
         const int nt = ls.tw * ls.th;

@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(256) slab_fill_kernel(const SlabParams s, int 
 }
 
 // ------------------------------------------------------------- the adjoint
-template <typename VT, bool MULTI>
+template <typename VT, bool MULTI, bool WARP_AGG>
 __global__ void __launch_bounds__(512, 1) raymarch_bwd_slab_kernel(const MarchParams p, const SlabParams s) {
     __shared__ int item_sh;
     const int total = s.counters[0];
@@ -226,9 +226,12 @@ __global__ void __launch_bounds__(512, 1) raymarch_bwd_slab_kernel(const MarchPa
         const int bt = it.x, k = it.y;
         const int b = bt / p.tm.tiles, tile = bt % p.tm.tiles;
         const int axis = s.axis[b];
-        const SlabCut cut{axis, k * s.Z[axis], (k + 1) * s.Z[axis]};
+        // selected, not indexed: a run-time index into the by-value kernel
+        // parameter would copy the parameter struct to local memory
+        const int thick = axis == 0 ? s.Z[0] : (axis == 1 ? s.Z[1] : s.Z[2]);
+        const SlabCut cut{axis, k * thick, (k + 1) * thick};
         const size_t slot = (size_t)s.offset[bt] + (size_t)(k - s.trange[bt].x);
-        bwd_body<VT, MULTI, true, false, 0, true, true>(p, tile, b, slot, cut);
+        bwd_body<VT, MULTI, true, false, 0, true, true, WARP_AGG>(p, tile, b, slot, cut);
     }
 }
 
@@ -265,8 +268,8 @@ __global__ void __launch_bounds__(256) slab_pose_reduce_kernel(const SlabParams 
 
 template <typename VT, bool MULTI>
 static cudaError_t launch_slab_march(const MarchParams& p, const SlabParams& s, unsigned block, size_t smem,
-                                     cudaStream_t st) {
-    auto kern = raymarch_bwd_slab_kernel<VT, MULTI>;
+                                     bool warp_agg, cudaStream_t st) {
+    auto kern = warp_agg ? raymarch_bwd_slab_kernel<VT, MULTI, true> : raymarch_bwd_slab_kernel<VT, MULTI, false>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
@@ -277,8 +280,12 @@ static cudaError_t launch_slab_march(const MarchParams& p, const SlabParams& s, 
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, (int)block, smem);
     if (e != cudaSuccess) return e;
     const unsigned grid = (unsigned)std::max(1, sms * std::max(per_sm, 1));
+    const KernelEvents& ev = kernel_events();
+    if (ev.start != nullptr) cudaEventRecord(ev.start, st);
     kern<<<grid, block, smem, st>>>(p, s);
-    return cudaGetLastError();
+    e = cudaGetLastError();
+    if (ev.stop != nullptr && e == cudaSuccess) e = cudaEventRecord(ev.stop, st);
+    return e;
 }
 
 // Slab-ordered adjoint with volume gradient for the quad layout; writes gM
@@ -317,17 +324,19 @@ cudaError_t launch_bwd_slab(const ndrr_raymarch_args& a, const LaunchShape& ls, 
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     const size_t smem = bwd_epilogue_bytes(a, ls);
     const bool multi = a.n_classes > 1;
+    const bool agg = a.gvol_mode == NDRR_GVOL_SLAB_WARP;
     switch (a.vol_dtype) {
         case NDRR_F32:
-            e = multi ? launch_slab_march<float, true>(p, s, R, smem, st) : launch_slab_march<float, false>(p, s, R, smem, st);
+            e = multi ? launch_slab_march<float, true>(p, s, R, smem, agg, st)
+                      : launch_slab_march<float, false>(p, s, R, smem, agg, st);
             break;
         case NDRR_F16:
-            e = multi ? launch_slab_march<__half, true>(p, s, R, smem, st)
-                      : launch_slab_march<__half, false>(p, s, R, smem, st);
+            e = multi ? launch_slab_march<__half, true>(p, s, R, smem, agg, st)
+                      : launch_slab_march<__half, false>(p, s, R, smem, agg, st);
             break;
         case NDRR_BF16:
-            e = multi ? launch_slab_march<__nv_bfloat16, true>(p, s, R, smem, st)
-                      : launch_slab_march<__nv_bfloat16, false>(p, s, R, smem, st);
+            e = multi ? launch_slab_march<__nv_bfloat16, true>(p, s, R, smem, agg, st)
+                      : launch_slab_march<__nv_bfloat16, false>(p, s, R, smem, agg, st);
             break;
         default: return cudaErrorInvalidValue;
     }

@@ -61,3 +61,38 @@ def rays_for(g, rt_key="rt_inv", ortho=False, device="cuda", dtype=torch.float32
 
 def np64(t) -> np.ndarray:
     return torch.as_tensor(t).detach().double().cpu().numpy()
+
+
+def load_reference_triton():
+    """The unmodified reference (baseline/_ref, installed by
+    baseline/install_reference.py) with its Triton backend, or (None, why).
+    Triton's bundled ptxas predates sm_103a, so the CUDA toolkit's ptxas is
+    named for it (TRITON_PTXAS_PATH) unless one is set."""
+    import os
+    import shutil
+    import sys
+    from pathlib import Path
+
+    ref_dir = Path(__file__).resolve().parents[1] / "baseline" / "_ref"
+    if not (ref_dir / "nanodrr").is_dir():
+        return None, "baseline/_ref is not installed"
+    if "TRITON_PTXAS_PATH" not in os.environ:
+        for cand in (shutil.which("ptxas"), "/usr/local/cuda/bin/ptxas"):
+            if cand and Path(cand).exists():
+                os.environ["TRITON_PTXAS_PATH"] = cand
+                break
+    try:
+        import triton  # noqa: F401
+    except Exception as e:
+        return None, f"triton is not importable: {e}"
+    if str(ref_dir) not in sys.path:
+        sys.path.insert(0, str(ref_dir))
+    try:
+        from nanodrr.data import Subject as RefSubject
+        from nanodrr.drr.renderer import _triton_available
+        from nanodrr.drr.renderer import render as ref_render
+    except Exception as e:
+        return None, f"the reference does not import: {e}"
+    if not _triton_available():
+        return None, "the reference's Triton backend does not import"
+    return {"Subject": RefSubject, "render": ref_render}, None

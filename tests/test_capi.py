@@ -62,7 +62,11 @@ def test_workspace_query_needs_no_gpu(lib):
     a = _valid_args()
     nb = ctypes.c_uint64()
     assert lib.ndrr_raymarch_bwd_workspace_bytes(ctypes.byref(a), ctypes.byref(nb)) == _ffi.NDRR_OK
-    # 8 x 8 image, default 16 x 8 tiles -> 1 tile per pose, 16 floats per tile
+    # 8 x 8 image of a small launch: default 8 x 4 tiles -> 2 tiles per pose,
+    # 16 floats per tile
+    assert nb.value == 2 * 2 * 16 * 4
+    a.tile_w, a.tile_h = 16, 8  # a chosen tile: 1 tile per pose
+    assert lib.ndrr_raymarch_bwd_workspace_bytes(ctypes.byref(a), ctypes.byref(nb)) == _ffi.NDRR_OK
     assert nb.value == 2 * 1 * 16 * 4
 
 
@@ -234,3 +238,13 @@ def test_quad_build_and_hu_to_mu_validate_on_the_host(lib):
         _ffi.NDRR_ERR_INVALID_ARGUMENT
     assert lib.ndrr_hu_to_mu(0x1000, _ffi.NDRR_U8, 4, 0.02, 0.05, 1000.0, 0x1000, None) == _ffi.NDRR_ERR_DTYPE
     assert lib.ndrr_hu_to_mu(None, _ffi.NDRR_F32, 0, 0.02, 0.05, 1000.0, None, None) == _ffi.NDRR_OK
+
+
+def test_measurement_entry_points_validate_on_the_host(lib):
+    assert lib.ndrr_set_kernel_events(0x1000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert lib.ndrr_set_kernel_events(None, None) == _ffi.NDRR_OK
+    assert lib.ndrr_l2_read_probe(None, 1024, 1, 0x2000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert lib.ndrr_l2_read_probe(0x1008, 1024, 1, 0x2000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert lib.ndrr_l2_read_probe(0x1000, 1024, 0, 0x2000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    flags = ctypes.c_uint32(0)
+    assert lib.ndrr_device_flags(None, 0) == _ffi.NDRR_ERR_INVALID_ARGUMENT

@@ -429,6 +429,11 @@ def test_slab_ordered_adjoint_equals_direct(dtype, C, seed):
     assert rel_maxabs(slab[0], direct[0]) < 1e-5
     assert rel_maxabs(slab[1], direct[1]) < 1e-5
     assert torch.equal(slab[1], again[1])
+    # gvol_mode 4: the same work with lanes that share a quad cell combining
+    # their terms before the reduction; the pose gradient is untouched
+    warp = raymarch_backward(*args, quad=q, gvol_mode=4)
+    assert rel_maxabs(warp[0], direct[0]) < 1e-5
+    assert torch.equal(warp[1], slab[1])
     if C == 1:  # (with labels, fp32-vs-fp64 label routing differs at label boundaries)
         ref = march_numpy_adjoint(go.double().cpu().numpy(), v.float().cpu().numpy().astype(np.float64), lab, M,
                                   src, tgt, step, n, C)
