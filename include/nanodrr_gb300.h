@@ -40,7 +40,7 @@
 extern "C" {
 #endif
 
-#define NDRR_ABI_VERSION 2
+#define NDRR_ABI_VERSION 3
 
 #if defined(__GNUC__)
 #define NDRR_API __attribute__((visibility("default")))
@@ -204,6 +204,15 @@ typedef struct ndrr_raymarch_args {
      * weights have 8 fractional bits (results differ from the fp32 path by
      * about 1e-3 relative); one channel, no skipping, no quad layout. */
     uint64_t vol_texture;
+
+    /* Labelled quad layout (16-bit volumes with n_classes in 2..255): set to
+     * 1 when vol_quad was built by ndrr_quad_build_labeled. Each 16-byte
+     * element then also carries its four corners' classes, so a per-label
+     * sample takes its nearest label from the two loads that bring its
+     * corners instead of a third gather from `lab` (same routing, same
+     * results). lab stays required and is what the other paths read. */
+    int32_t quad_labels;
+    int32_t reserved0;
 } ndrr_raymarch_args;
 
 /* Forward variants (ndrr_raymarch_args.fwd_mode). */
@@ -447,6 +456,17 @@ NDRR_API int32_t ndrr_batched_bwd(const ndrr_batch_args* args, void* stream);
 NDRR_API int32_t ndrr_quad_dims(int32_t D, int32_t H, int32_t W, int32_t* qz, int32_t* qy, int32_t* qx);
 NDRR_API int32_t ndrr_quad_build(const void* vol, int32_t vol_dtype, int32_t D, int32_t H, int32_t W, void* quad,
                                  void* stream);
+
+/* Labelled quad layout of a 16-bit (f16 / bf16) volume and its label map
+ * (any ndrr_dtype, truncated toward zero like a cast): the same extent, 16
+ * bytes per element — the four corner values of ndrr_quad_build's 8-byte
+ * element, then the four corners' classes as uint8 (a class in [0,
+ * n_classes) as is, 255 for a label outside it, 0 for a corner outside the
+ * volume), then 4 zero bytes. n_classes in 2..255. Use with quad_labels = 1.
+ * No counterpart in the reference. */
+NDRR_API int32_t ndrr_quad_build_labeled(const void* vol, int32_t vol_dtype, const void* lab, int32_t lab_dtype,
+                                         int32_t n_classes, int32_t D, int32_t H, int32_t W, void* quad,
+                                         void* stream);
 
 /* HU -> linear attenuation (1/mm) of n elements, elementwise: replaces the
  * reference's hu_to_mu (src/nanodrr/data/preprocess.py:9-50), which Subject

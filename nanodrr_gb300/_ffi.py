@@ -26,7 +26,7 @@ NDRR_FLAG_TMA_TIMEOUT = 1
 # ndrr_dtype
 NDRR_F32, NDRR_F16, NDRR_BF16, NDRR_U8, NDRR_I8, NDRR_I16, NDRR_I32, NDRR_I64 = range(8)
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 
 # ndrr_gvol_mode
 NDRR_GVOL_AUTO, NDRR_GVOL_DIRECT, NDRR_GVOL_BRICK, NDRR_GVOL_SLAB, NDRR_GVOL_SLAB_WARP = 0, 1, 2, 3, 4
@@ -94,6 +94,8 @@ class RaymarchArgs(ctypes.Structure):
         ("fwd_mode", ctypes.c_int32),
         ("gvol_overwrite", ctypes.c_int32),
         ("vol_texture", ctypes.c_uint64),
+        ("quad_labels", ctypes.c_int32),
+        ("reserved0", ctypes.c_int32),
     ]
 
     def __init__(self, **kw):
@@ -149,6 +151,8 @@ SIGNATURES: dict[str, tuple] = {
     "ndrr_batched_bwd": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p]),
     "ndrr_quad_dims": (ctypes.c_int32, [ctypes.c_int32] * 3 + [_i32p] * 3),
     "ndrr_quad_build": (ctypes.c_int32, [ctypes.c_void_p] + [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 2),
+    "ndrr_quad_build_labeled": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]
+                                + [ctypes.c_int32] * 5 + [ctypes.c_void_p] * 2),
     "ndrr_hu_to_mu": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
                                        ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]),
     "ndrr_set_kernel_events": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p]),

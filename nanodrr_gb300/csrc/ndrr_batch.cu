@@ -77,9 +77,9 @@ __global__ void __launch_bounds__(256, 4) batched_fwd_kernel(const BatchParams b
         const int r = find_request(bp.off, bp.n_req, item);
         const MarchParams p = request_params(bp, bp.req[r], r);
         if (p.quad != nullptr)
-            fwd_body<VT, VT, MULTI, 0, true>(p, item - __ldg(bp.off + r), 0);
+            fwd_body<VT, VT, MULTI, 0, kLayoutQuad>(p, item - __ldg(bp.off + r), 0);
         else
-            fwd_body<VT, VT, MULTI, 0, false>(p, item - __ldg(bp.off + r), 0);
+            fwd_body<VT, VT, MULTI, 0, kLayoutVolume>(p, item - __ldg(bp.off + r), 0);
     }
 }
 
@@ -96,9 +96,9 @@ __global__ void __launch_bounds__(256, 2) batched_bwd_kernel(const BatchParams b
         const MarchParams p = request_params(bp, bp.req[r], r);
         const int tile = item - __ldg(bp.off + r);
         if (p.quad != nullptr)
-            bwd_body<VT, MULTI, false, GCAM, 0, true>(p, tile, 0, (size_t)tile);
+            bwd_body<VT, MULTI, false, GCAM, 0, kLayoutQuad>(p, tile, 0, (size_t)tile);
         else
-            bwd_body<VT, MULTI, false, GCAM, 0, false>(p, tile, 0, (size_t)tile);
+            bwd_body<VT, MULTI, false, GCAM, 0, kLayoutVolume>(p, tile, 0, (size_t)tile);
     }
 }
 

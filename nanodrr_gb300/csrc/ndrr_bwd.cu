@@ -34,16 +34,16 @@ template <typename VT, bool MULTI, bool GCAM>
 static cudaError_t bwd_dispatch_skip(const MarchParams& p, int skip, unsigned grid, unsigned block, size_t smem,
                                      cudaStream_t st) {
     if (skip == NDRR_SKIP_OCCUPANCY)
-        return launch_kernel(raymarch_bwd_kernel<VT, MULTI, false, GCAM, 1, false>, grid, block, smem, st, p);
-    return launch_kernel(raymarch_bwd_kernel<VT, MULTI, false, GCAM, 0, false>, grid, block, smem, st, p);
+        return launch_kernel(raymarch_bwd_kernel<VT, MULTI, false, GCAM, 1, kLayoutVolume>, grid, block, smem, st, p);
+    return launch_kernel(raymarch_bwd_kernel<VT, MULTI, false, GCAM, 0, kLayoutVolume>, grid, block, smem, st, p);
 }
 
 template <typename VT, bool MULTI>
 static cudaError_t bwd_dispatch_flags(const MarchParams& p, bool gvol, bool gcam, int skip, unsigned grid,
                                       unsigned block, size_t smem, cudaStream_t st) {
     // With a volume gradient every sample matters: skipping never applies.
-    if (gvol && gcam) return launch_kernel(raymarch_bwd_kernel<VT, MULTI, true, true, 0, false>, grid, block, smem, st, p);
-    if (gvol) return launch_kernel(raymarch_bwd_kernel<VT, MULTI, true, false, 0, false>, grid, block, smem, st, p);
+    if (gvol && gcam) return launch_kernel(raymarch_bwd_kernel<VT, MULTI, true, true, 0, kLayoutVolume>, grid, block, smem, st, p);
+    if (gvol) return launch_kernel(raymarch_bwd_kernel<VT, MULTI, true, false, 0, kLayoutVolume>, grid, block, smem, st, p);
     if (gcam) return bwd_dispatch_skip<VT, MULTI, true>(p, skip, grid, block, smem, st);
     return bwd_dispatch_skip<VT, MULTI, false>(p, skip, grid, block, smem, st);
 }
@@ -75,7 +75,8 @@ cudaError_t launch_bwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaS
             if (e == cudaSuccess) e = launch_quad_fold(a.gvol_quad, a.D, a.H, a.W, a.gvol, a.gvol_overwrite != 0, st);
             return e;
         }
-        e = launch_bwd_quad(p, a.vol_dtype, multi, gvol, gcam, skip, grid, block, bwd_smem_bytes(a, ls), st);
+        e = launch_bwd_quad(p, a.vol_dtype, multi, gvol, gcam, skip, a.quad_labels != 0, grid, block,
+                            bwd_smem_bytes(a, ls), st);
         if (e == cudaSuccess && gvol) e = launch_quad_fold(a.gvol_quad, a.D, a.H, a.W, a.gvol, a.gvol_overwrite != 0, st);
     } else if (gvol && ls.brick) {
         e = launch_brick(a, ls, p, grid, block, st);

@@ -168,6 +168,13 @@ int32_t validate_common(const ndrr_raymarch_args* a) {
         return fail(NDRR_ERR_INVALID_ARGUMENT, "brick capacity %d out of range [0, 57344] voxels", a->brick_cap);
     if (a->slab_mib < 0 || a->slab_mib > 4096)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "slab size %d MiB out of range [0, 4096]", a->slab_mib);
+    if (a->quad_labels != 0) {
+        if (a->quad_labels != 1 || a->vol_quad == nullptr)
+            return fail(NDRR_ERR_INVALID_ARGUMENT, "quad_labels is 0, or 1 with a labelled quad in vol_quad");
+        if (a->vol_dtype == NDRR_F32 || a->n_classes < 2 || a->n_classes > 255)
+            return fail(NDRR_ERR_INVALID_ARGUMENT,
+                        "the labelled quad layout is for f16/bf16 volumes with n_classes in 2..255");
+    }
     return NDRR_OK;
 }
 
@@ -197,7 +204,7 @@ extern "C" {
 int32_t ndrr_abi_version(void) { return NDRR_ABI_VERSION; }
 
 const char* ndrr_build_info(void) {
-    return "nanodrr_gb300 abi " "2" " sm_103a nvcc " __DATE__;
+    return "nanodrr_gb300 abi " "3" " sm_103a nvcc " __DATE__;
 }
 
 const char* ndrr_last_error(void) { return g_last_error.c_str(); }
@@ -484,6 +491,26 @@ int32_t ndrr_quad_build(const void* vol, int32_t dtype, int32_t D, int32_t H, in
     if (rc != NDRR_OK) return rc;
     const cudaError_t e = ndrr::launch_quad_build(vol, dtype, D, H, W, quad, reinterpret_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "quad build failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
+int32_t ndrr_quad_build_labeled(const void* vol, int32_t dtype, const void* lab, int32_t lab_dtype, int32_t n_classes,
+                                int32_t D, int32_t H, int32_t W, void* quad, void* stream) {
+    if (vol == nullptr || lab == nullptr || quad == nullptr)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "vol, lab and quad must be non-NULL");
+    if (dtype != NDRR_F16 && dtype != NDRR_BF16)
+        return fail(NDRR_ERR_DTYPE, "the labelled quad layout takes f16 or bf16 volumes (got dtype %d)", dtype);
+    if (!is_any_dtype(lab_dtype)) return fail(NDRR_ERR_DTYPE, "label dtype %d unsupported", lab_dtype);
+    if (n_classes < 2 || n_classes > 255)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "n_classes must be 2..255 (got %d)", n_classes);
+    if (misaligned(quad, 16) || misaligned(vol, 2) || misaligned(lab, dtype_bytes(lab_dtype)))
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "quad must be 16-byte aligned, vol and lab aligned to their elements");
+    int32_t qz, qy, qx;
+    const int32_t rc = ndrr_quad_dims(D, H, W, &qz, &qy, &qx);
+    if (rc != NDRR_OK) return rc;
+    const cudaError_t e = ndrr::launch_quad_build_labeled(vol, dtype, lab, lab_dtype, n_classes, D, H, W, quad,
+                                                          reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "labelled quad build failed: %s", cudaGetErrorString(e));
     return ok();
 }
 

@@ -150,6 +150,7 @@ struct Cell {
     float v000, v001, v010, v011, v100, v101, v110, v111;  // v[z][y][x] offsets
     float fx, fy, fz;
     int ix, iy, iz;
+    int cls;  // labelled quad layout only: class of the nearest corner (255 = dropped)
 };
 
 template <typename VT>
@@ -293,6 +294,36 @@ __device__ __forceinline__ void load_cell_quad(const void* __restrict__ quad, co
         unpack_quad_f16(q0, c.v000, c.v001, c.v010, c.v011);
         unpack_quad_f16(q1, c.v100, c.v101, c.v110, c.v111);
     }
+}
+
+// Labelled quad layout (16-bit volumes): a 16-byte element holds the four
+// corner values of the plain 16-bit quad in .x/.y and the four corners'
+// classes (uint8, in the same corner order; 255 = dropped, 0 outside the
+// volume) in .z; .w is zero. The two loads of a sample then also carry the
+// classes of its eight corners, and the nearest one is picked by rounding:
+// the corner offsets rint(p) - cell index (ties to even, the reference's
+// nearest rule) are 0 or 1 on every axis, because positions are clamped into
+// the padded extent first exactly as nearest_label clamps them.
+template <typename VT>
+__device__ __forceinline__ void load_cell_quad_labeled(const void* __restrict__ quad, const QuadGeom& g, int D, int H,
+                                                       int W, float x, float y, float z, Cell& c) {
+    const int qi = quad_cell(g, D, H, W, x, y, z, c);
+    const uint4* __restrict__ qp = reinterpret_cast<const uint4*>(quad);
+    const uint4 q0 = __ldg(qp + qi);
+    const uint4 q1 = __ldg(qp + qi + g.plane);
+    if constexpr (std::is_same<VT, __nv_bfloat16>::value) {
+        unpack_quad_bf16(make_uint2(q0.x, q0.y), c.v000, c.v001, c.v010, c.v011);
+        unpack_quad_bf16(make_uint2(q1.x, q1.y), c.v100, c.v101, c.v110, c.v111);
+    } else {
+        unpack_quad_f16(make_uint2(q0.x, q0.y), c.v000, c.v001, c.v010, c.v011);
+        unpack_quad_f16(make_uint2(q1.x, q1.y), c.v100, c.v101, c.v110, c.v111);
+    }
+    const float xc = fminf(fmaxf(x, -2.0f), (float)W + 1.0f);
+    const float yc = fminf(fmaxf(y, -2.0f), (float)H + 1.0f);
+    const float zc = fminf(fmaxf(z, -2.0f), (float)D + 1.0f);
+    const int ox = (int)rintf(xc) - c.ix, oy = (int)rintf(yc) - c.iy, oz = (int)rintf(zc) - c.iz;
+    const unsigned labels = oz ? q1.z : q0.z;
+    c.cls = (int)((labels >> (8 * (ox + 2 * oy))) & 0xffu);
 }
 
 __device__ __forceinline__ float cell_value(const Cell& c) {

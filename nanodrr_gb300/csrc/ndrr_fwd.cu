@@ -12,11 +12,11 @@ static cudaError_t fwd_dispatch_skip(const MarchParams& p, int skip, unsigned gr
                                      cudaStream_t st) {
     if constexpr (std::is_same<VT, OT>::value) {
         if (skip == NDRR_SKIP_OCCUPANCY)
-            return launch_kernel(raymarch_fwd_kernel<VT, OT, MULTI, 1, false>, grid, block, smem, st, p);
+            return launch_kernel(raymarch_fwd_kernel<VT, OT, MULTI, 1, kLayoutVolume>, grid, block, smem, st, p);
     } else {
         if (skip != NDRR_SKIP_NONE) return cudaErrorNotSupported;
     }
-    return launch_kernel(raymarch_fwd_kernel<VT, OT, MULTI, 0, false>, grid, block, smem, st, p);
+    return launch_kernel(raymarch_fwd_kernel<VT, OT, MULTI, 0, kLayoutVolume>, grid, block, smem, st, p);
 }
 
 template <typename VT, typename OT>
@@ -46,7 +46,7 @@ cudaError_t launch_fwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaS
     const int skip = a.skip_mode;
     if (a.vol_quad != nullptr) {
         if (a.out_dtype != a.vol_dtype) return cudaErrorNotSupported;
-        return launch_fwd_quad(p, a.vol_dtype, multi, skip, grid, block, smem, st);
+        return launch_fwd_quad(p, a.vol_dtype, multi, skip, a.quad_labels != 0, grid, block, smem, st);
     }
     switch (a.vol_dtype) {
         case NDRR_F32: return fwd_dispatch_out<float>(p, a.out_dtype, multi, skip, grid, block, smem, st);

@@ -204,11 +204,18 @@ __device__ __forceinline__ void skip_stats_add(const MarchParams& p, unsigned lo
     }
 }
 
+// Volume layouts a kernel reads (the QUAD template argument).
+constexpr int kLayoutVolume = 0;   // the caller's [D, H, W] array, eight gathers
+constexpr int kLayoutQuad = 1;     // quad layout, two vector loads
+constexpr int kLayoutQuadLab = 2;  // labelled quad layout (16-bit volumes): classes ride in the same loads
+
 // The eight corners of the sample's cell from the plain volume (bounds
-// checked per corner) or from the quad layout (two vector loads).
-template <typename VT, bool QUAD>
+// checked per corner) or from the quad layouts (two vector loads).
+template <typename VT, int QUAD>
 __device__ __forceinline__ void fetch_cell(const MarchParams& p, float x, float y, float z, Cell& c) {
-    if constexpr (QUAD) {
+    if constexpr (QUAD == kLayoutQuadLab) {
+        load_cell_quad_labeled<VT>(p.quad, p.qg, p.D, p.H, p.W, x, y, z, c);
+    } else if constexpr (QUAD == kLayoutQuad) {
         load_cell_quad<VT>(p.quad, p.qg, p.D, p.H, p.W, x, y, z, c);
     } else {
         load_cell(reinterpret_cast<const VT*>(p.vol), p.D, p.H, p.W, x, y, z, c);
@@ -217,7 +224,7 @@ __device__ __forceinline__ void fetch_cell(const MarchParams& p, float x, float 
 
 // ===================================================================== forward
 // SKIP: 0 no skipping (or precomputed sample windows), 1 occupancy window.
-template <typename VT, typename OT, bool MULTI, int SKIP, bool QUAD = false>
+template <typename VT, typename OT, bool MULTI, int SKIP, int QUAD = kLayoutVolume>
 __device__ __forceinline__ void fwd_body(const MarchParams& p, const int tile, const int b) {
     extern __shared__ float smem[];
     const int R = p.tw * p.th;
@@ -264,7 +271,12 @@ __device__ __forceinline__ void fwd_body(const MarchParams& p, const int tile, c
             }
         }
         if (MULTI) {
-            const int cls = nearest_label(p.lab, p.lab_dtype, p.D, p.H, p.W, x, y, z);
+            int cls;
+            if constexpr (QUAD == kLayoutQuadLab) {
+                cls = cell.cls;
+            } else {
+                cls = nearest_label(p.lab, p.lab_dtype, p.D, p.H, p.W, x, y, z);
+            }
             if ((unsigned)cls < (unsigned)p.C) cacc[cls * NT] += val;
         }
     }
@@ -319,7 +331,7 @@ __device__ __forceinline__ void fwd_body(const MarchParams& p, const int tile, c
     }
 }
 
-template <typename VT, typename OT, bool MULTI, int SKIP, bool QUAD>
+template <typename VT, typename OT, bool MULTI, int SKIP, int QUAD>
 __global__ void __launch_bounds__(512, 2) raymarch_fwd_kernel(const MarchParams p) {
     fwd_body<VT, OT, MULTI, SKIP, QUAD>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles);
 }
@@ -485,12 +497,15 @@ struct QuadScatterWarp {
 // Upstream gradient of one sample: the ray's own for one channel, else the
 // one of the sample's label channel, with out-of-range labels masked like
 // the forward drops them (_fused.py:233-237).
+__device__ __forceinline__ float class_go(const MarchParams& p, int b, const ThreadRay& tr, int cls) {
+    return ((unsigned)cls < (unsigned)p.C) ? ld_any_f(p.go, p.go_dtype, ((size_t)b * p.C + cls) * p.N + tr.n) : 0.f;
+}
+
 template <bool MULTI>
 __device__ __forceinline__ float sample_go(const MarchParams& p, int b, const ThreadRay& tr, float go_ray, float x,
                                            float y, float z) {
     if (!MULTI) return go_ray;
-    const int cls = nearest_label(p.lab, p.lab_dtype, p.D, p.H, p.W, x, y, z);
-    return ((unsigned)cls < (unsigned)p.C) ? ld_any_f(p.go, p.go_dtype, ((size_t)b * p.C + cls) * p.N + tr.n) : 0.f;
+    return class_go(p, b, tr, nearest_label(p.lab, p.lab_dtype, p.D, p.H, p.W, x, y, z));
 }
 
 // Adjoint terms of one sample whose cell is loaded.
@@ -502,12 +517,36 @@ __device__ __forceinline__ void adjoint_accumulate(const float (&m)[12], const T
 // Samples go in pairs: both pairs' loads are issued before either's
 // reductions, so two gathers per thread are in flight. The accumulation
 // order is the sample order either way.
-template <typename VT, bool MULTI, bool GVOL, bool GCAM, typename Scatter, bool QUAD = false>
+template <typename VT, bool MULTI, bool GVOL, bool GCAM, typename Scatter, int QUAD = kLayoutVolume>
 __device__ __forceinline__ void adjoint_samples(const MarchParams& p, const float (&m)[12], const ThreadRay& tr,
                                                 int b, int s0, int s1, float go_ray, AdjAcc& A,
                                                 const Scatter& scatter) {
     if (!MULTI && go_ray == 0.f) return;  // every term is proportional to go
     int s = s0;
+    if constexpr (QUAD == kLayoutQuadLab) {
+        // the class of a sample arrives with its corners: fetch, then route
+        for (; s + 1 < s1; s += 2) {
+            const float ta = (float)s * p.inv_s, tb = (float)(s + 1) * p.inv_s;
+            Cell ca, cb;
+            fetch_cell<VT, QUAD>(p, fmaf(ta, tr.ray.dx, tr.ray.p0x), fmaf(ta, tr.ray.dy, tr.ray.p0y),
+                                 fmaf(ta, tr.ray.dz, tr.ray.p0z), ca);
+            fetch_cell<VT, QUAD>(p, fmaf(tb, tr.ray.dx, tr.ray.p0x), fmaf(tb, tr.ray.dy, tr.ray.p0y),
+                                 fmaf(tb, tr.ray.dz, tr.ray.p0z), cb);
+            const float ga = MULTI ? class_go(p, b, tr, ca.cls) : go_ray;
+            const float gb = MULTI ? class_go(p, b, tr, cb.cls) : go_ray;
+            if (ga != 0.f) adjoint_accumulate<GVOL, GCAM>(m, tr, ta, ga, ca, A, scatter);
+            if (gb != 0.f) adjoint_accumulate<GVOL, GCAM>(m, tr, tb, gb, cb, A, scatter);
+        }
+        if (s < s1) {
+            const float t = (float)s * p.inv_s;
+            Cell cell;
+            fetch_cell<VT, QUAD>(p, fmaf(t, tr.ray.dx, tr.ray.p0x), fmaf(t, tr.ray.dy, tr.ray.p0y),
+                                 fmaf(t, tr.ray.dz, tr.ray.p0z), cell);
+            const float gg = MULTI ? class_go(p, b, tr, cell.cls) : go_ray;
+            if (gg != 0.f) adjoint_accumulate<GVOL, GCAM>(m, tr, t, gg, cell, A, scatter);
+        }
+        return;
+    }
     for (; s + 1 < s1; s += 2) {
         const float ta = (float)s * p.inv_s, tb = (float)(s + 1) * p.inv_s;
         const float xa = fmaf(ta, tr.ray.dx, tr.ray.p0x), xb = fmaf(tb, tr.ray.dx, tr.ray.p0x);
@@ -694,7 +733,7 @@ __device__ __forceinline__ void restrict_to_slab(const MarchParams& p, ThreadRay
     r.hi = e;
 }
 
-template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP, bool QUAD = false, bool SLAB = false,
+template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP, int QUAD = kLayoutVolume, bool SLAB = false,
           bool WARP_AGG = false>
 __device__ __forceinline__ void bwd_body(const MarchParams& p, const int tile, const int b, const size_t slot,
                                          const SlabCut cut = SlabCut{0, 0, 0}) {
@@ -721,12 +760,12 @@ __device__ __forceinline__ void bwd_body(const MarchParams& p, const int tile, c
 
     AdjAcc A;
     A.zero();
-    if constexpr (QUAD && WARP_AGG) {
+    if constexpr (QUAD != kLayoutVolume && WARP_AGG) {
         const QuadScatterWarp sc{p.gquad, p.qg};
-        adjoint_samples<VT, MULTI, GVOL, GCAM, QuadScatterWarp, true>(p, m, tr, b, tr.s0, tr.s1, go_ray, A, sc);
-    } else if constexpr (QUAD) {
+        adjoint_samples<VT, MULTI, GVOL, GCAM, QuadScatterWarp, QUAD>(p, m, tr, b, tr.s0, tr.s1, go_ray, A, sc);
+    } else if constexpr (QUAD != kLayoutVolume) {
         const QuadScatter sc{p.gquad, p.qg};
-        adjoint_samples<VT, MULTI, GVOL, GCAM, QuadScatter, true>(p, m, tr, b, tr.s0, tr.s1, go_ray, A, sc);
+        adjoint_samples<VT, MULTI, GVOL, GCAM, QuadScatter, QUAD>(p, m, tr, b, tr.s0, tr.s1, go_ray, A, sc);
     } else {
         const DirectScatter sc{p.gvol, p.D, p.H, p.W};
         adjoint_samples<VT, MULTI, GVOL, GCAM>(p, m, tr, b, tr.s0, tr.s1, go_ray, A, sc);
@@ -734,7 +773,7 @@ __device__ __forceinline__ void bwd_body(const MarchParams& p, const int tile, c
     adjoint_epilogue<GCAM>(p, slot, tr, A, smem, R, NT, r, k);
 }
 
-template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP, bool QUAD>
+template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP, int QUAD>
 __global__ void __launch_bounds__(512, 1) raymarch_bwd_kernel(const MarchParams p) {
     bwd_body<VT, MULTI, GVOL, GCAM, SKIP, QUAD>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles, blockIdx.x);
 }
@@ -880,12 +919,14 @@ __global__ void __launch_bounds__(256, 2) raymarch_bwd_brick_kernel(const MarchP
 cudaError_t launch_brick(const ndrr_raymarch_args& a, const LaunchShape& ls, const MarchParams& p, unsigned grid,
                          unsigned block, cudaStream_t st);
 // Quad-layout instantiations live in their own translation units.
-cudaError_t launch_fwd_quad(const MarchParams& p, int vol_dtype, bool multi, int skip, unsigned grid,
+cudaError_t launch_fwd_quad(const MarchParams& p, int vol_dtype, bool multi, int skip, bool labeled, unsigned grid,
                             unsigned block, size_t smem, cudaStream_t st);
 cudaError_t launch_bwd_quad(const MarchParams& p, int vol_dtype, bool multi, bool gvol, bool gcam, int skip,
-                            unsigned grid, unsigned block, size_t smem, cudaStream_t st);
+                            bool labeled, unsigned grid, unsigned block, size_t smem, cudaStream_t st);
 cudaError_t launch_quad_fold(const float* gquad, int D, int H, int W, float* gvol, bool overwrite, cudaStream_t st);
 cudaError_t launch_quad_build(const void* vol, int dtype, int D, int H, int W, void* quad, cudaStream_t st);
+cudaError_t launch_quad_build_labeled(const void* vol, int dtype, const void* lab, int lab_dtype, int C, int D, int H,
+                                      int W, void* quad, cudaStream_t st);
 
 MarchParams make_params(const ndrr_raymarch_args& a, const LaunchShape& ls);
 cudaError_t launch_bwd_slab(const ndrr_raymarch_args& a, const LaunchShape& ls, const MarchParams& p,

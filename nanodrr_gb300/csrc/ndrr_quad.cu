@@ -49,6 +49,35 @@ __global__ void quad_build_b16_kernel(const uint16_t* __restrict__ v, int D, int
     }
 }
 
+// 16-bit volume + label map -> labelled quads: the four raw 16-bit corner
+// values as in quad_build_b16_kernel, and the four corners' classes (class
+// in [0, C) as uint8, 255 for a label outside it; 0 for a corner outside the
+// volume, the class the nearest-label rule gives a position there).
+__global__ void quad_build_labeled_kernel(const uint16_t* __restrict__ v, const void* __restrict__ lab,
+                                          int lab_dtype, int C, int D, int H, int W, uint4* __restrict__ q) {
+    const int QX = W + 3, QY = H + 3;
+    const long long n = (long long)(D + 4) * QY * QX;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const int qx = (int)(i % QX), qy = (int)((i / QX) % QY), qz = (int)(i / ((long long)QX * QY));
+        const int x0 = qx - 2, y0 = qy - 2, z = qz - 2;
+        uint32_t c[4] = {0u, 0u, 0u, 0u};
+        uint32_t labels = 0u;
+        if ((unsigned)z < (unsigned)D) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int x = x0 + (k & 1), y = y0 + (k >> 1);
+                if ((unsigned)x < (unsigned)W && (unsigned)y < (unsigned)H) {
+                    const int idx = (z * H + y) * W + x;
+                    c[k] = v[idx];
+                    const int cls = ld_label(lab, lab_dtype, idx);
+                    labels |= (uint32_t)((unsigned)cls < (unsigned)C ? cls : 255) << (8 * k);
+                }
+            }
+        }
+        q[i] = make_uint4(c[0] | (c[1] << 16), c[2] | (c[3] << 16), labels, 0u);
+    }
+}
+
 // gvol[z][y][x] += the four quad entries in which voxel (x, y) of plane z is
 // a corner: (x, y) as (x0, y0), (x0 + 1, y0), (x0, y0 + 1), (x0 + 1, y0 + 1).
 // One CTA per kFoldRows consecutive lines (z, y) of the volume, four
@@ -142,6 +171,15 @@ cudaError_t launch_quad_build(const void* vol, int dtype, int D, int H, int W, v
         quad_build_b16_kernel<<<grid_for(n), 256, 0, st>>>((const uint16_t*)vol, D, H, W, (uint2*)quad);
     else
         return cudaErrorInvalidValue;
+    return cudaGetLastError();
+}
+
+cudaError_t launch_quad_build_labeled(const void* vol, int dtype, const void* lab, int lab_dtype, int C, int D, int H,
+                                      int W, void* quad, cudaStream_t st) {
+    if (dtype != NDRR_F16 && dtype != NDRR_BF16) return cudaErrorInvalidValue;
+    const long long n = (long long)(D + 4) * (H + 3) * (W + 3);
+    quad_build_labeled_kernel<<<grid_for(n), 256, 0, st>>>((const uint16_t*)vol, lab, lab_dtype, C, D, H, W,
+                                                           (uint4*)quad);
     return cudaGetLastError();
 }
 

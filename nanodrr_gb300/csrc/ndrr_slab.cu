@@ -212,7 +212,7 @@ __global__ void __launch_bounds__(256) slab_fill_kernel(const SlabParams s, int 
 }
 
 // ------------------------------------------------------------- the adjoint
-template <typename VT, bool MULTI, bool WARP_AGG>
+template <typename VT, bool MULTI, bool WARP_AGG, int LAYOUT>
 __global__ void __launch_bounds__(512, 1) raymarch_bwd_slab_kernel(const MarchParams p, const SlabParams s) {
     __shared__ int item_sh;
     const int total = s.counters[0];
@@ -231,7 +231,7 @@ __global__ void __launch_bounds__(512, 1) raymarch_bwd_slab_kernel(const MarchPa
         const int thick = axis == 0 ? s.Z[0] : (axis == 1 ? s.Z[1] : s.Z[2]);
         const SlabCut cut{axis, k * thick, (k + 1) * thick};
         const size_t slot = (size_t)s.offset[bt] + (size_t)(k - s.trange[bt].x);
-        bwd_body<VT, MULTI, true, false, 0, true, true, WARP_AGG>(p, tile, b, slot, cut);
+        bwd_body<VT, MULTI, true, false, 0, LAYOUT, true, WARP_AGG>(p, tile, b, slot, cut);
     }
 }
 
@@ -266,10 +266,11 @@ __global__ void __launch_bounds__(256) slab_pose_reduce_kernel(const SlabParams 
     }
 }
 
-template <typename VT, bool MULTI>
+template <typename VT, bool MULTI, int LAYOUT = kLayoutQuad>
 static cudaError_t launch_slab_march(const MarchParams& p, const SlabParams& s, unsigned block, size_t smem,
                                      bool warp_agg, cudaStream_t st) {
-    auto kern = warp_agg ? raymarch_bwd_slab_kernel<VT, MULTI, true> : raymarch_bwd_slab_kernel<VT, MULTI, false>;
+    auto kern = warp_agg ? raymarch_bwd_slab_kernel<VT, MULTI, true, LAYOUT>
+                         : raymarch_bwd_slab_kernel<VT, MULTI, false, LAYOUT>;
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
@@ -325,18 +326,21 @@ cudaError_t launch_bwd_slab(const ndrr_raymarch_args& a, const LaunchShape& ls, 
     const size_t smem = bwd_epilogue_bytes(a, ls);
     const bool multi = a.n_classes > 1;
     const bool agg = a.gvol_mode == NDRR_GVOL_SLAB_WARP;
+    const bool lab_quad = a.quad_labels != 0 && multi;  // validated: 16-bit volume with label channels
     switch (a.vol_dtype) {
         case NDRR_F32:
             e = multi ? launch_slab_march<float, true>(p, s, R, smem, agg, st)
                       : launch_slab_march<float, false>(p, s, R, smem, agg, st);
             break;
         case NDRR_F16:
-            e = multi ? launch_slab_march<__half, true>(p, s, R, smem, agg, st)
-                      : launch_slab_march<__half, false>(p, s, R, smem, agg, st);
+            e = lab_quad ? launch_slab_march<__half, true, kLayoutQuadLab>(p, s, R, smem, agg, st)
+                : multi  ? launch_slab_march<__half, true>(p, s, R, smem, agg, st)
+                         : launch_slab_march<__half, false>(p, s, R, smem, agg, st);
             break;
         case NDRR_BF16:
-            e = multi ? launch_slab_march<__nv_bfloat16, true>(p, s, R, smem, agg, st)
-                      : launch_slab_march<__nv_bfloat16, false>(p, s, R, smem, agg, st);
+            e = lab_quad ? launch_slab_march<__nv_bfloat16, true, kLayoutQuadLab>(p, s, R, smem, agg, st)
+                : multi  ? launch_slab_march<__nv_bfloat16, true>(p, s, R, smem, agg, st)
+                         : launch_slab_march<__nv_bfloat16, false>(p, s, R, smem, agg, st);
             break;
         default: return cudaErrorInvalidValue;
     }

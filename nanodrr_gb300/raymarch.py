@@ -209,6 +209,48 @@ def quad_volume(vol: torch.Tensor, out: torch.Tensor | None = None) -> torch.Ten
     return q
 
 
+def quad_volume_labeled(vol: torch.Tensor, lab: torch.Tensor, n_classes: int,
+                        out: torch.Tensor | None = None) -> torch.Tensor:
+    """Labelled quad-layout copy of a 16-bit [D, H, W] volume and its label
+    map (see ndrr_quad_build_labeled): 16 bytes per element, the quad's four
+    corner values and the four corners' classes, so a per-label sample reads
+    its nearest label from the two loads that bring its corners. Pass it as
+    `quad` to the march (recognised by its size). n_classes in 2..255."""
+    if not vol.is_cuda or vol.dim() != 3 or vol.dtype not in (torch.float16, torch.bfloat16):
+        raise ValueError("quad_volume_labeled needs a [D, H, W] float16/bfloat16 CUDA tensor")
+    if tuple(lab.shape) != tuple(vol.shape) or lab.device != vol.device:
+        raise ValueError("the label map must match the volume's shape and device")
+    if not 2 <= n_classes <= 255:
+        raise ValueError("the labelled quad layout takes 2..255 classes")
+    vol, lab = vol.contiguous(), lab.contiguous()
+    D, H, W = vol.shape
+    nbytes = (D + 4) * (H + 3) * (W + 3) * 16
+    if out is not None:
+        if out.dtype != torch.uint8 or out.numel() != nbytes or out.device != vol.device or not out.is_contiguous():
+            raise ValueError("out is not a labelled quad copy of a volume of this shape")
+        q = out
+    else:
+        q = torch.empty(nbytes, device=vol.device, dtype=torch.uint8)
+    lib = _ffi.load()
+    _ffi.check(
+        lib.ndrr_quad_build_labeled(vol.data_ptr(), ndrr_dtype(vol), lab.data_ptr(), ndrr_dtype(lab), n_classes,
+                                    D, H, W, q.data_ptr(), _stream_handle(vol.device)),
+        "ndrr_quad_build_labeled",
+    )
+    return q
+
+
+def quad_is_labeled(vol: torch.Tensor, quad: torch.Tensor) -> bool:
+    """Whether `quad` is the labelled quad copy of `vol` (16 bytes per element
+    for a 16-bit volume) rather than the plain one; any other size raises."""
+    D, H, W = vol.shape
+    n = (D + 4) * (H + 3) * (W + 3)
+    es = quad.numel() // n if n else 0
+    if quad.numel() != n * es or es not in ((16,) if vol.dtype == torch.float32 else (8, 16)):
+        raise ValueError("quad is not a quad-layout copy of a volume of this shape and dtype")
+    return vol.dtype != torch.float32 and es == 16
+
+
 class TextureVolume:
     """Hardware-filtered 3-D texture of a float32 [D, H, W] volume
     (ndrr_texture_create) for the texture forward variant: pass it as
@@ -304,6 +346,7 @@ def raymarch_forward(
         a.sample_window = _ptr(windows)
     if quad is not None and quad.numel():
         a.vol_quad = quad.data_ptr()
+        a.quad_labels = int(quad_is_labeled(vol, quad))
     a.fwd_mode = int(fwd_mode)
     if texture is not None:
         if texture.shape != tuple(vol.shape) or texture.device != vol.device or not texture.handle:
@@ -414,6 +457,7 @@ def raymarch_backward(
     a.gvol_overwrite = int(overwrite)
     if quad_on:
         a.vol_quad = quad.data_ptr()
+        a.quad_labels = int(quad_is_labeled(vol, quad))
         if need_gvol:
             D, H, W = vol.shape
             gq = torch.empty((D + 4) * (H + 3) * (W + 3) * 4, device=dev, dtype=torch.float32)

@@ -20,8 +20,7 @@ import torch
 
 from . import _ffi
 from .geometry import convert, mm_small, transform_point
-from .raymarch import quad_volume
-from .renderer import render
+from .renderer import build_quad, quad_cache_key, render
 
 
 class Registration(torch.nn.Module):
@@ -295,6 +294,7 @@ class GraphedStep:
         sub = reg.subject
         cache = getattr(sub, "_ndrr_quad_cache", None)
         self._quad = cache[1] if cache is not None else None
+        self._quad_labels = (cache[2], cache[3]) if cache is not None else (None, 1)
         # The volume tensor the graph reads, held so that its memory cannot be
         # freed and handed to another tensor while the graph can replay.
         self._vol = sub.image
@@ -323,9 +323,10 @@ class GraphedStep:
             return
         vol = img.reshape(img.shape[-3:]) if img.shape[:2] == (1, 1) else img[0, 0]
         if self._quad is not None:
-            quad_volume(vol.detach(), out=self._quad)
-            key = (vol.data_ptr(), vol._version, vol.dtype, tuple(vol.shape), vol.device)
-            object.__setattr__(sub, "_ndrr_quad_cache", (key, self._quad))
+            lab, n_classes = self._quad_labels
+            build_quad(vol, lab, n_classes, out=self._quad)
+            object.__setattr__(sub, "_ndrr_quad_cache",
+                               (quad_cache_key(vol, lab, n_classes), self._quad, lab, n_classes))
         skip = getattr(sub, "empty_space", None)
         if skip is not None:
             skip.grid.refresh(vol)

@@ -17,7 +17,14 @@ import weakref
 
 import torch
 
-from .raymarch import fused_raymarch, fused_raymarch_ex, fused_raymarch_ex_forward, quad_volume, raymarch_forward
+from .raymarch import (
+    fused_raymarch,
+    fused_raymarch_ex,
+    fused_raymarch_ex_forward,
+    quad_volume,
+    quad_volume_labeled,
+    raymarch_forward,
+)
 from .subject import Subject
 
 _BACKENDS = ("auto", "cuda", "triton")
@@ -128,7 +135,7 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
     if skip is None and layout == "plain":
         out = raymarch_forward(*args)[0] if direct else fused_raymarch(*args)
     else:
-        quad = cached_quad(subject, vol) if layout == "quad" else vol.new_empty(0, dtype=torch.uint8)
+        quad = cached_quad(subject, vol, lab, C) if layout == "quad" else vol.new_empty(0, dtype=torch.uint8)
         empty = vol.new_empty(0, dtype=torch.uint8)
         if skip is not None:
             sk = (skip.grid.grid, skip.grid.cell, skip.packed, int(skip.mode), float(skip.margin),
@@ -141,15 +148,35 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
     return out.reshape(B, C, height, width)
 
 
-def cached_quad(subject, vol: torch.Tensor) -> torch.Tensor:
-    """The volume's quad-layout copy, rebuilt whenever the volume tensor or
-    its contents (version counter) change."""
+def labeled_quad_applies(vol: torch.Tensor, n_classes: int) -> bool:
+    """Per-label renders of 16-bit volumes read the labelled quad layout:
+    the class of a sample rides in the loads of its corners."""
+    return vol.dtype in (torch.float16, torch.bfloat16) and 2 <= n_classes <= 255
+
+
+def quad_cache_key(vol: torch.Tensor, lab: torch.Tensor | None, n_classes: int) -> tuple:
     key = (vol.data_ptr(), vol._version, vol.dtype, tuple(vol.shape), vol.device)
+    if lab is not None and labeled_quad_applies(vol, n_classes):
+        key += (lab.data_ptr(), lab._version, lab.dtype, n_classes)
+    return key
+
+
+def build_quad(vol: torch.Tensor, lab: torch.Tensor | None, n_classes: int, out: torch.Tensor | None = None):
+    if lab is not None and labeled_quad_applies(vol, n_classes):
+        return quad_volume_labeled(vol.detach(), lab, n_classes, out=out)
+    return quad_volume(vol.detach(), out=out)
+
+
+def cached_quad(subject, vol: torch.Tensor, lab: torch.Tensor | None = None, n_classes: int = 1) -> torch.Tensor:
+    """The volume's quad-layout copy (labelled with `lab`'s classes for a
+    per-label render of a 16-bit volume), rebuilt whenever the volume or
+    label tensor or their contents (version counters) change."""
+    key = quad_cache_key(vol, lab, n_classes)
     cache = getattr(subject, "_ndrr_quad_cache", None)
     if cache is not None and cache[0] == key:
         return cache[1]
-    q = quad_volume(vol.detach())
-    object.__setattr__(subject, "_ndrr_quad_cache", (key, q))
+    q = build_quad(vol, lab, n_classes)
+    object.__setattr__(subject, "_ndrr_quad_cache", (key, q, lab, n_classes))
     return q
 
 

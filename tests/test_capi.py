@@ -42,7 +42,7 @@ def test_abi_version_and_struct_layout(lib):
     assert lib.ndrr_abi_version() == _ffi.ABI_VERSION
     assert b"sm_103a" in lib.ndrr_build_info()
     # 64-bit layout of ndrr_raymarch_args as declared in the header
-    assert ctypes.sizeof(_ffi.RaymarchArgs) == 344
+    assert ctypes.sizeof(_ffi.RaymarchArgs) == 352
     assert ctypes.sizeof(_ffi.OccupancyArgs) == 56
 
 
@@ -248,3 +248,22 @@ def test_measurement_entry_points_validate_on_the_host(lib):
     assert lib.ndrr_l2_read_probe(0x1000, 1024, 0, 0x2000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
     flags = ctypes.c_uint32(0)
     assert lib.ndrr_device_flags(None, 0) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+
+
+def test_labelled_quad_validates_on_the_host(lib):
+    a = _valid_args()
+    a.vol_quad, a.quad_labels = 0x7000, 1  # f32 volume: not for the labelled layout
+    a.n_classes, a.lab, a.lab_dtype = 3, 0x6000, _ffi.NDRR_U8
+    assert lib.ndrr_raymarch_fwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert "labelled" in lib.ndrr_last_error().decode()
+    a.vol_dtype, a.n_classes = _ffi.NDRR_BF16, 1  # one channel: no labels to carry
+    assert lib.ndrr_raymarch_fwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    a.quad_labels, a.vol_quad = 1, None
+    assert lib.ndrr_raymarch_fwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    b = lib.ndrr_quad_build_labeled
+    assert b(0x1000, _ffi.NDRR_F32, 0x2000, _ffi.NDRR_U8, 3, 4, 4, 4, 0x3000, None) == _ffi.NDRR_ERR_DTYPE
+    assert b(0x1000, _ffi.NDRR_BF16, 0x2000, _ffi.NDRR_U8, 1, 4, 4, 4, 0x3000, None) == \
+        _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert b(0x1000, _ffi.NDRR_BF16, 0x2000, _ffi.NDRR_U8, 3, 4, 4, 4, 0x3008, None) == \
+        _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert b(0x1000, _ffi.NDRR_BF16, None, _ffi.NDRR_U8, 3, 4, 4, 4, 0x3000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT

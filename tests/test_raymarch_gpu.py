@@ -616,3 +616,61 @@ def test_slab_axis_choices_equal_direct(axis_dir):
     slab = raymarch_backward(*args, quad=q, gvol_mode=3, slab_mib=1)
     assert rel_maxabs(slab[0], direct[0]) < 1e-5
     assert rel_maxabs(slab[1], direct[1]) < 1e-5
+
+
+@pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16])
+@pytest.mark.parametrize("lab_dtype", [torch.uint8, torch.float32])
+def test_labelled_quad_equals_quad_with_label_gathers(dtype, lab_dtype):
+    """The labelled quad layout carries each corner's class in the 16-byte
+    element: the per-label forward (with the total) is bitwise the plain quad
+    layout's with label gathers, the adjoint's pose gradient bitwise, its
+    volume gradient to atomics rounding — through the direct and the
+    slab-ordered adjoints, with the out-of-range class value dropped and
+    rays that leave the volume."""
+    from nanodrr_gb300.raymarch import quad_volume, quad_volume_labeled
+
+    n, C = 190, 5
+    vol, lab, M, src, tgt, step, width = _random_case(83, B=3, Hd=20, Wd=24, vol_shape=(40, 36, 44), C=C)
+    t = lambda a: torch.from_numpy(a).to(DEV)  # noqa: E731
+    v = t(vol).to(dtype)
+    lb = t(lab).to(lab_dtype)
+    q = quad_volume(v)
+    ql = quad_volume_labeled(v, lb, C)
+    assert ql.numel() == 2 * q.numel()
+    args = (v, lb, t(M), t(src), t(tgt), t(step), n, C, width)
+    ref, ref_total = raymarch_forward(*args, quad=q, with_total=True)
+    out, total = raymarch_forward(*args, quad=ql, with_total=True)
+    assert torch.equal(out, ref) and torch.equal(total, ref_total)
+    assert float(out.float().abs().max()) > 0
+    go = torch.randn(3, C, 20 * 24, device=DEV)
+    for mode, gcam in ((1, True), (3, False)):
+        bargs = (go, *args, True, gcam)
+        a = raymarch_backward(*bargs, quad=q, gvol_mode=mode)
+        b = raymarch_backward(*bargs, quad=ql, gvol_mode=mode)
+        assert torch.equal(a[1], b[1])
+        assert rel_maxabs(b[0], a[0]) < 1e-5
+        if gcam:
+            for ga, gb in zip(a[2:], b[2:]):
+                assert torch.equal(ga, gb)
+
+
+def test_labelled_quad_is_the_render_path_for_16_bit_per_label_volumes():
+    """render() of a bf16 subject with labels reads the labelled quad, and its
+    image equals the plain-layout render's."""
+    from nanodrr_gb300 import phantom
+    from nanodrr_gb300.renderer import cached_quad, compact_label
+
+    ph = phantom.make_phantom((40, 40, 40), (128 / 40,) * 3, seed=4)
+    sub = ph.subject(dtype=torch.bfloat16, with_labels=True, device=DEV)
+    k_inv, sdd = phantom.detector(pixel=1.4 * 200 / 32, height=32, width=32)
+    rt = phantom.random_poses(2, seed=9).to(DEV)
+    k_inv, sdd = k_inv.to(DEV), sdd.to(DEV)
+    with torch.no_grad():
+        out = nd.render(sub, k_inv, rt, sdd, 32, 32, n_samples=300)
+        vol = sub.image[0, 0]
+        q = cached_quad(sub, vol, compact_label(sub), sub.n_classes)
+        assert q.numel() == (40 + 4) * 43 * 43 * 16  # labelled elements
+        sub.layout = "plain"
+        plain = nd.render(sub, k_inv, rt, sdd, 32, 32, n_samples=300)
+    assert rel_maxabs(out.float(), plain.float()) < 1e-2  # bf16 output rounding of fp32 sums
+    assert torch.equal(out.float().sum(1).abs() > 0, plain.float().sum(1).abs() > 0)
