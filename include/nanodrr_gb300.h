@@ -21,6 +21,8 @@
  * Coordinate conventions (identical to the reference renderer):
  *   - the volume is a dense row-major [D, H, W] array; voxel (x, y, z) is
  *     element (z * H + y) * W + x;
+ *   - sample positions are computed from the inputs in float-float and
+ *     carried in 32.32 fixed point, not rounded to float32 (see M_lo);
  *   - M is a per-pose 3x4 row-major affine from camera space (mm) to voxel
  *     index space, so sample s of ray n sits at
  *         p = M @ [lerp(src_n, tgt_n, t_s), 1],  t_s = s / (n_samples - 1);
@@ -213,6 +215,14 @@ typedef struct ndrr_raymarch_args {
      * results). lab stays required and is what the other paths read. */
     int32_t quad_labels;
     int32_t reserved0;
+
+    /* Optional low parts of M, [B, 3, 4] f32, or NULL: the affine is taken as
+     * M + M_lo (a float64 affine split into two floats, ~2^-48 relative).
+     * Sample positions are formed from it in float-float and carried in 32.32
+     * fixed point (about 2e-7 voxel after 800 samples), so a sample falls in
+     * the cell the exact position falls in; with M_lo NULL the float32 M is
+     * taken as exact. */
+    const float* M_lo;
 } ndrr_raymarch_args;
 
 /* Forward variants (ndrr_raymarch_args.fwd_mode). */

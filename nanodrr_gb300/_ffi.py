@@ -96,6 +96,7 @@ class RaymarchArgs(ctypes.Structure):
         ("vol_texture", ctypes.c_uint64),
         ("quad_labels", ctypes.c_int32),
         ("reserved0", ctypes.c_int32),
+        ("M_lo", ctypes.c_void_p),
     ]
 
     def __init__(self, **kw):

@@ -75,6 +75,7 @@ int32_t validate_alignment(const ndrr_raymarch_args* a) {
         {a->vol, ve, "vol"},
         {a->n_classes > 1 ? a->lab : nullptr, dtype_bytes(a->lab_dtype), "lab"},
         {a->M, 4, "M"},
+        {a->M_lo, 4, "M_lo"},
         {a->src, 4, "src"},
         {a->tgt, 4, "tgt"},
         {a->step, 4, "step"},

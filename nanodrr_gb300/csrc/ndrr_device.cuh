@@ -143,6 +143,85 @@ __device__ __forceinline__ void apply_t_window(Ray& r, float wlo, float whi, int
     r.hi = min(r.hi, (int)b);
 }
 
+// ------------------------------------------------- fixed-point ray positions
+// A sample's position p0 + s * step (voxel index space) is carried in 32.32
+// fixed point: int64 counts of 2^-32 voxel. The cell is the integer part and
+// the trilinear weights come from the fractional part, so a position keeps
+// 2^-32 voxel resolution anywhere in the volume, where a float keeps 2^-9 at
+// 512 (ulp 6.1e-5 voxel). This matters for the gradients: the trilinear
+// derivative jumps at every cell face, and float positions put about one
+// sample in 10^4 on the other side of a face than the exact (float64)
+// position does, which moves pose gradients at the 1e-3 level. The start p0
+// and the step are formed per ray in float-float arithmetic (error-free
+// products and sums on fp32, about 44 significant bits) from the inputs, so
+// positions match the float64 oracle's to ~2e-7 voxel after 800 samples.
+struct FixPos {
+    long long x, y, z;
+};
+
+__device__ __forceinline__ int fix_floor(long long v) { return (int)(v >> 32); }
+
+// The top 23 bits of the fraction, exactly, as a float in [0, 1).
+__device__ __forceinline__ float fix_frac(long long v) {
+    return __int_as_float(0x3f800000u | ((unsigned)v >> 9)) - 1.0f;
+}
+
+// Nearest integer, ties to even (the nearest-label rule), on the exact value.
+__device__ __forceinline__ int fix_round(long long v) {
+    const int f = fix_floor(v);
+    const unsigned lo = (unsigned)v;
+    return f + ((lo > 0x80000000u) || (lo == 0x80000000u && (f & 1)) ? 1 : 0);
+}
+
+__device__ __forceinline__ FixPos fix_add(const FixPos& a, const FixPos& b) {
+    return FixPos{a.x + b.x, a.y + b.y, a.z + b.z};
+}
+
+// Float-float helpers (value = hi + lo) for the per-ray set-up, written with
+// _rn intrinsics so the compiler cannot contract or reorder them.
+struct F2 {
+    float hi, lo;
+};
+
+__device__ __forceinline__ F2 f2_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return F2{s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
+}
+
+__device__ __forceinline__ F2 f2_norm(float hi, float lo) {
+    const float s = __fadd_rn(hi, lo);
+    return F2{s, __fsub_rn(lo, __fsub_rn(s, hi))};
+}
+
+__device__ __forceinline__ F2 f2_add(F2 a, F2 b) {
+    const F2 s = f2_two_sum(a.hi, b.hi);
+    return f2_norm(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+__device__ __forceinline__ F2 f2_mul(F2 a, F2 b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);  // exact error of the product
+    e = __fmaf_rn(a.hi, b.lo, __fmaf_rn(a.lo, b.hi, e));
+    return f2_norm(p, e);
+}
+
+// a / n for an integer n exactly representable in fp32: the remainder of the
+// leading quotient is exact with an FMA.
+__device__ __forceinline__ F2 f2_div_int(F2 a, float n) {
+    const float q = __fdiv_rn(a.hi, n);
+    const float r = __fmaf_rn(-q, n, a.hi);
+    return f2_norm(q, __fdiv_rn(__fadd_rn(r, a.lo), n));
+}
+
+// float-float -> 32.32 fixed point, clamped to +-2^30 voxels (a ray that far
+// out has an empty window anyway); hi * 2^32 and lo * 2^32 are exact scalings.
+__device__ __forceinline__ long long f2_to_fix(F2 v) {
+    const float hi = fminf(fmaxf(v.hi, -1073741824.0f), 1073741824.0f);
+    const float lo = hi == v.hi ? v.lo : 0.0f;
+    return __float2ll_rn(__fmul_rn(hi, 4294967296.0f)) + __float2ll_rn(__fmul_rn(lo, 4294967296.0f));
+}
+
 // ------------------------------------------------------------ trilinear tap
 // The eight corners of the cell containing (x, y, z), zero outside the volume,
 // and the fractional offsets inside the cell.
@@ -152,49 +231,6 @@ struct Cell {
     int ix, iy, iz;
     int cls;  // labelled quad layout only: class of the nearest corner (255 = dropped)
 };
-
-template <typename VT>
-__device__ __forceinline__ void load_cell(const VT* __restrict__ vol, int D, int H, int W, float x, float y,
-                                          float z, Cell& c) {
-    // Positions are clamped to [-2, dim + 1] first: beyond that every corner
-    // is outside the volume either way, and the clamp keeps the float -> int
-    // conversion in range for any input.
-    x = fminf(fmaxf(x, -2.0f), (float)W + 1.0f);
-    y = fminf(fmaxf(y, -2.0f), (float)H + 1.0f);
-    z = fminf(fmaxf(z, -2.0f), (float)D + 1.0f);
-    const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
-    c.fx = x - xf;
-    c.fy = y - yf;
-    c.fz = z - zf;
-    const int ix = (int)xf, iy = (int)yf, iz = (int)zf;
-    c.ix = ix;
-    c.iy = iy;
-    c.iz = iz;
-    const int HW = H * W;
-    const int base = (iz * H + iy) * W + ix;
-    if ((unsigned)ix < (unsigned)(W - 1) && (unsigned)iy < (unsigned)(H - 1) && (unsigned)iz < (unsigned)(D - 1)) {
-        c.v000 = ld_vox(vol, base);
-        c.v001 = ld_vox(vol, base + 1);
-        c.v010 = ld_vox(vol, base + W);
-        c.v011 = ld_vox(vol, base + W + 1);
-        c.v100 = ld_vox(vol, base + HW);
-        c.v101 = ld_vox(vol, base + HW + 1);
-        c.v110 = ld_vox(vol, base + HW + W);
-        c.v111 = ld_vox(vol, base + HW + W + 1);
-    } else {
-        const bool x0 = (unsigned)ix < (unsigned)W, x1 = (unsigned)(ix + 1) < (unsigned)W;
-        const bool y0 = (unsigned)iy < (unsigned)H, y1 = (unsigned)(iy + 1) < (unsigned)H;
-        const bool z0 = (unsigned)iz < (unsigned)D, z1 = (unsigned)(iz + 1) < (unsigned)D;
-        c.v000 = (z0 && y0 && x0) ? ld_vox(vol, base) : 0.f;
-        c.v001 = (z0 && y0 && x1) ? ld_vox(vol, base + 1) : 0.f;
-        c.v010 = (z0 && y1 && x0) ? ld_vox(vol, base + W) : 0.f;
-        c.v011 = (z0 && y1 && x1) ? ld_vox(vol, base + W + 1) : 0.f;
-        c.v100 = (z1 && y0 && x0) ? ld_vox(vol, base + HW) : 0.f;
-        c.v101 = (z1 && y0 && x1) ? ld_vox(vol, base + HW + 1) : 0.f;
-        c.v110 = (z1 && y1 && x0) ? ld_vox(vol, base + HW + W) : 0.f;
-        c.v111 = (z1 && y1 && x1) ? ld_vox(vol, base + HW + W + 1) : 0.f;
-    }
-}
 
 // ------------------------------------------------------------ quad layout
 // A padded copy of the volume in which element (qz, qy, qx) holds the four
@@ -258,74 +294,6 @@ __device__ __forceinline__ void unpack_quad_f16(uint2 q, float& a, float& b, flo
     d = f1.y;
 }
 
-// Quad index of the cell whose lower corner is the floor of (x, y, z),
-// clamped into the padded extent, plus the fractional offsets and the cell's
-// (clamped) corner indices for the gradient scatter.
-__device__ __forceinline__ int quad_cell(const QuadGeom& g, int D, int H, int W, float x, float y, float z,
-                                         Cell& c) {
-    x = fminf(fmaxf(x, -2.0f), (float)W + 1.0f);
-    y = fminf(fmaxf(y, -2.0f), (float)H + 1.0f);
-    z = fminf(fmaxf(z, -2.0f), (float)D + 1.0f);
-    const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
-    c.fx = x - xf;
-    c.fy = y - yf;
-    c.fz = z - zf;
-    c.ix = min((int)xf, W);
-    c.iy = min((int)yf, H);
-    c.iz = min((int)zf, D);
-    return ((c.iz + 2) * g.qy + (c.iy + 2)) * g.qx + (c.ix + 2);
-}
-
-template <typename VT>
-__device__ __forceinline__ void load_cell_quad(const void* __restrict__ quad, const QuadGeom& g, int D, int H,
-                                               int W, float x, float y, float z, Cell& c) {
-    const int qi = quad_cell(g, D, H, W, x, y, z, c);
-    using Q = typename QuadOf<VT>::T;
-    const Q* __restrict__ qp = reinterpret_cast<const Q*>(quad);
-    const Q q0 = __ldg(qp + qi);
-    const Q q1 = __ldg(qp + qi + g.plane);
-    if constexpr (std::is_same<VT, float>::value) {
-        unpack_quad(q0, c.v000, c.v001, c.v010, c.v011);
-        unpack_quad(q1, c.v100, c.v101, c.v110, c.v111);
-    } else if constexpr (std::is_same<VT, __nv_bfloat16>::value) {
-        unpack_quad_bf16(q0, c.v000, c.v001, c.v010, c.v011);
-        unpack_quad_bf16(q1, c.v100, c.v101, c.v110, c.v111);
-    } else {
-        unpack_quad_f16(q0, c.v000, c.v001, c.v010, c.v011);
-        unpack_quad_f16(q1, c.v100, c.v101, c.v110, c.v111);
-    }
-}
-
-// Labelled quad layout (16-bit volumes): a 16-byte element holds the four
-// corner values of the plain 16-bit quad in .x/.y and the four corners'
-// classes (uint8, in the same corner order; 255 = dropped, 0 outside the
-// volume) in .z; .w is zero. The two loads of a sample then also carry the
-// classes of its eight corners, and the nearest one is picked by rounding:
-// the corner offsets rint(p) - cell index (ties to even, the reference's
-// nearest rule) are 0 or 1 on every axis, because positions are clamped into
-// the padded extent first exactly as nearest_label clamps them.
-template <typename VT>
-__device__ __forceinline__ void load_cell_quad_labeled(const void* __restrict__ quad, const QuadGeom& g, int D, int H,
-                                                       int W, float x, float y, float z, Cell& c) {
-    const int qi = quad_cell(g, D, H, W, x, y, z, c);
-    const uint4* __restrict__ qp = reinterpret_cast<const uint4*>(quad);
-    const uint4 q0 = __ldg(qp + qi);
-    const uint4 q1 = __ldg(qp + qi + g.plane);
-    if constexpr (std::is_same<VT, __nv_bfloat16>::value) {
-        unpack_quad_bf16(make_uint2(q0.x, q0.y), c.v000, c.v001, c.v010, c.v011);
-        unpack_quad_bf16(make_uint2(q1.x, q1.y), c.v100, c.v101, c.v110, c.v111);
-    } else {
-        unpack_quad_f16(make_uint2(q0.x, q0.y), c.v000, c.v001, c.v010, c.v011);
-        unpack_quad_f16(make_uint2(q1.x, q1.y), c.v100, c.v101, c.v110, c.v111);
-    }
-    const float xc = fminf(fmaxf(x, -2.0f), (float)W + 1.0f);
-    const float yc = fminf(fmaxf(y, -2.0f), (float)H + 1.0f);
-    const float zc = fminf(fmaxf(z, -2.0f), (float)D + 1.0f);
-    const int ox = (int)rintf(xc) - c.ix, oy = (int)rintf(yc) - c.iy, oz = (int)rintf(zc) - c.iz;
-    const unsigned labels = oz ? q1.z : q0.z;
-    c.cls = (int)((labels >> (8 * (ox + 2 * oy))) & 0xffu);
-}
-
 __device__ __forceinline__ float cell_value(const Cell& c) {
     const float c00 = fmaf(c.fx, c.v001 - c.v000, c.v000);
     const float c01 = fmaf(c.fx, c.v011 - c.v010, c.v010);
@@ -353,14 +321,110 @@ __device__ __forceinline__ void cell_grad(const Cell& c, float& gx, float& gy, f
     gz = fmaf(z11, c.fy, __fmul_rn(z00, wy0));
 }
 
-// Nearest-voxel label at (x, y, z); ties round to even like grid_sample's
-// nearest mode. Out-of-volume positions read label 0 (zero padding).
-__device__ __forceinline__ int nearest_label(const void* __restrict__ lab, int lab_dtype, int D, int H, int W,
-                                             float x, float y, float z) {
-    x = fminf(fmaxf(x, -2.0f), (float)W + 1.0f);
-    y = fminf(fmaxf(y, -2.0f), (float)H + 1.0f);
-    z = fminf(fmaxf(z, -2.0f), (float)D + 1.0f);
-    const int rx = (int)rintf(x), ry = (int)rintf(y), rz = (int)rintf(z);
+// Cell of a fixed-point position: the integer parts clamped into [-2, dim]
+// (a cell there has every corner outside the volume, so the clamp changes no
+// value or gradient, and it keeps quad indices inside the padded extent) and
+// the fractions of the unclamped position.
+__device__ __forceinline__ void fix_cell(const FixPos& P, int D, int H, int W, Cell& c) {
+    c.ix = min(max(fix_floor(P.x), -2), W);
+    c.iy = min(max(fix_floor(P.y), -2), H);
+    c.iz = min(max(fix_floor(P.z), -2), D);
+    c.fx = fix_frac(P.x);
+    c.fy = fix_frac(P.y);
+    c.fz = fix_frac(P.z);
+}
+
+template <typename VT>
+__device__ __forceinline__ void load_cell_fix(const VT* __restrict__ vol, int D, int H, int W, const FixPos& P,
+                                              Cell& c) {
+    fix_cell(P, D, H, W, c);
+    const int ix = c.ix, iy = c.iy, iz = c.iz;
+    const int HW = H * W;
+    const int base = (iz * H + iy) * W + ix;
+    if ((unsigned)ix < (unsigned)(W - 1) && (unsigned)iy < (unsigned)(H - 1) && (unsigned)iz < (unsigned)(D - 1)) {
+        c.v000 = ld_vox(vol, base);
+        c.v001 = ld_vox(vol, base + 1);
+        c.v010 = ld_vox(vol, base + W);
+        c.v011 = ld_vox(vol, base + W + 1);
+        c.v100 = ld_vox(vol, base + HW);
+        c.v101 = ld_vox(vol, base + HW + 1);
+        c.v110 = ld_vox(vol, base + HW + W);
+        c.v111 = ld_vox(vol, base + HW + W + 1);
+    } else {
+        const bool x0 = (unsigned)ix < (unsigned)W, x1 = (unsigned)(ix + 1) < (unsigned)W;
+        const bool y0 = (unsigned)iy < (unsigned)H, y1 = (unsigned)(iy + 1) < (unsigned)H;
+        const bool z0 = (unsigned)iz < (unsigned)D, z1 = (unsigned)(iz + 1) < (unsigned)D;
+        c.v000 = (z0 && y0 && x0) ? ld_vox(vol, base) : 0.f;
+        c.v001 = (z0 && y0 && x1) ? ld_vox(vol, base + 1) : 0.f;
+        c.v010 = (z0 && y1 && x0) ? ld_vox(vol, base + W) : 0.f;
+        c.v011 = (z0 && y1 && x1) ? ld_vox(vol, base + W + 1) : 0.f;
+        c.v100 = (z1 && y0 && x0) ? ld_vox(vol, base + HW) : 0.f;
+        c.v101 = (z1 && y0 && x1) ? ld_vox(vol, base + HW + 1) : 0.f;
+        c.v110 = (z1 && y1 && x0) ? ld_vox(vol, base + HW + W) : 0.f;
+        c.v111 = (z1 && y1 && x1) ? ld_vox(vol, base + HW + W + 1) : 0.f;
+    }
+}
+
+__device__ __forceinline__ int quad_index(const QuadGeom& g, const Cell& c) {
+    return ((c.iz + 2) * g.qy + (c.iy + 2)) * g.qx + (c.ix + 2);
+}
+
+template <typename VT>
+__device__ __forceinline__ void load_cell_quad_fix(const void* __restrict__ quad, const QuadGeom& g, int D, int H,
+                                                   int W, const FixPos& P, Cell& c) {
+    fix_cell(P, D, H, W, c);
+    const int qi = quad_index(g, c);
+    using Q = typename QuadOf<VT>::T;
+    const Q* __restrict__ qp = reinterpret_cast<const Q*>(quad);
+    const Q q0 = __ldg(qp + qi);
+    const Q q1 = __ldg(qp + qi + g.plane);
+    if constexpr (std::is_same<VT, float>::value) {
+        unpack_quad(q0, c.v000, c.v001, c.v010, c.v011);
+        unpack_quad(q1, c.v100, c.v101, c.v110, c.v111);
+    } else if constexpr (std::is_same<VT, __nv_bfloat16>::value) {
+        unpack_quad_bf16(q0, c.v000, c.v001, c.v010, c.v011);
+        unpack_quad_bf16(q1, c.v100, c.v101, c.v110, c.v111);
+    } else {
+        unpack_quad_f16(q0, c.v000, c.v001, c.v010, c.v011);
+        unpack_quad_f16(q1, c.v100, c.v101, c.v110, c.v111);
+    }
+}
+
+// Labelled quad layout (16-bit volumes): a 16-byte element holds the four
+// corner values of the plain 16-bit quad in .x/.y and the four corners'
+// classes (uint8, in the same corner order; 255 = dropped, 0 outside the
+// volume) in .z; .w is zero. The two loads of a sample then also carry the
+// classes of its eight corners, and the nearest one is picked by rounding the
+// exact position (ties to even, the reference's nearest rule): its offsets
+// from the cell are 0 or 1 on each axis for any position the clamp left
+// alone; any other offset means the nearest voxel is outside the volume,
+// class 0.
+template <typename VT>
+__device__ __forceinline__ void load_cell_quad_labeled_fix(const void* __restrict__ quad, const QuadGeom& g, int D,
+                                                           int H, int W, const FixPos& P, Cell& c) {
+    fix_cell(P, D, H, W, c);
+    const int qi = quad_index(g, c);
+    const uint4* __restrict__ qp = reinterpret_cast<const uint4*>(quad);
+    const uint4 q0 = __ldg(qp + qi);
+    const uint4 q1 = __ldg(qp + qi + g.plane);
+    if constexpr (std::is_same<VT, __nv_bfloat16>::value) {
+        unpack_quad_bf16(make_uint2(q0.x, q0.y), c.v000, c.v001, c.v010, c.v011);
+        unpack_quad_bf16(make_uint2(q1.x, q1.y), c.v100, c.v101, c.v110, c.v111);
+    } else {
+        unpack_quad_f16(make_uint2(q0.x, q0.y), c.v000, c.v001, c.v010, c.v011);
+        unpack_quad_f16(make_uint2(q1.x, q1.y), c.v100, c.v101, c.v110, c.v111);
+    }
+    const int ox = fix_round(P.x) - c.ix, oy = fix_round(P.y) - c.iy, oz = fix_round(P.z) - c.iz;
+    const bool inside = (unsigned)ox <= 1u && (unsigned)oy <= 1u && (unsigned)oz <= 1u;
+    const unsigned labels = oz ? q1.z : q0.z;
+    c.cls = inside ? (int)((labels >> (8 * (ox + 2 * oy))) & 0xffu) : 0;
+}
+
+// Nearest-voxel label at a fixed-point position (ties to even); positions
+// whose nearest voxel is outside the volume read label 0 (zero padding).
+__device__ __forceinline__ int nearest_label_fix(const void* __restrict__ lab, int lab_dtype, int D, int H, int W,
+                                                 const FixPos& P) {
+    const int rx = fix_round(P.x), ry = fix_round(P.y), rz = fix_round(P.z);
     if ((unsigned)rx < (unsigned)W && (unsigned)ry < (unsigned)H && (unsigned)rz < (unsigned)D)
         return ld_label(lab, lab_dtype, (rz * H + ry) * W + rx);
     return 0;

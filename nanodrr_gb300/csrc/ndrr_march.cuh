@@ -42,6 +42,7 @@ struct MarchParams {
     int lab_dtype;
     int C;
     const float* M;
+    const float* M_lo;  // optional low parts: M + M_lo is the affine to ~2^-48 (NULL: M is exact)
     const float* src;
     const float* tgt;
     const float* step;
@@ -89,7 +90,37 @@ struct ThreadRay {
     float stepv;   // camera-space sample spacing
     float sx, sy, sz, ex, ey, ez;  // camera-space source and src -> tgt
     int s0, s1;    // this thread's sample chunk
+    FixPos f0, fd;  // voxel-space position of sample 0 and the step per sample, 32.32 fixed point
 };
+
+// Fixed-point start and step of a ray: p0 = M [src, 1] and step = M [tgt -
+// src, 0] / (S - 1) in float-float from the float32 inputs (tgt - src exactly,
+// M as M + M_lo), converted to 32.32 fixed point.
+__device__ __forceinline__ void fix_ray(const MarchParams& p, const float (&m)[12], int b, float sx, float sy,
+                                        float sz, float tx, float ty, float tz, ThreadRay& tr) {
+    const F2 e[3] = {f2_two_sum(tx, -sx), f2_two_sum(ty, -sy), f2_two_sum(tz, -sz)};
+    const F2 src[3] = {F2{sx, 0.f}, F2{sy, 0.f}, F2{sz, 0.f}};
+    const float n1 = (float)(p.S - 1);
+    long long f0[3], fd[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        F2 row[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) row[j] = F2{m[4 * i + j], p.M_lo ? __ldg(p.M_lo + (size_t)b * 12 + 4 * i + j) : 0.f};
+        const F2 d = f2_add(f2_add(f2_mul(row[0], e[0]), f2_mul(row[1], e[1])), f2_mul(row[2], e[2]));
+        const F2 q = f2_add(f2_add(f2_add(f2_mul(row[0], src[0]), f2_mul(row[1], src[1])), f2_mul(row[2], src[2])),
+                            row[3]);
+        f0[i] = f2_to_fix(q);
+        fd[i] = f2_to_fix(f2_div_int(d, n1));
+    }
+    tr.f0 = FixPos{f0[0], f0[1], f0[2]};
+    tr.fd = FixPos{fd[0], fd[1], fd[2]};
+}
+
+// Fixed-point position of sample s.
+__device__ __forceinline__ FixPos fix_at(const ThreadRay& tr, int s) {
+    return FixPos{tr.f0.x + (long long)s * tr.fd.x, tr.f0.y + (long long)s * tr.fd.y, tr.f0.z + (long long)s * tr.fd.z};
+}
 
 // Box-culled ray set-up (every thread of a ray computes the same window).
 __device__ __forceinline__ void init_thread_ray(const MarchParams& p, const float (&m)[12], int b, int n,
@@ -99,6 +130,7 @@ __device__ __forceinline__ void init_thread_ray(const MarchParams& p, const floa
     tr.stepv = 0.f;
     tr.sx = tr.sy = tr.sz = tr.ex = tr.ey = tr.ez = 0.f;
     tr.ray.p0x = tr.ray.p0y = tr.ray.p0z = tr.ray.dx = tr.ray.dy = tr.ray.dz = 0.f;
+    tr.f0 = tr.fd = FixPos{0, 0, 0};
     tr.bn = 0;
     if (n >= 0) {
         const size_t bn = (size_t)b * p.N + n;
@@ -115,6 +147,7 @@ __device__ __forceinline__ void init_thread_ray(const MarchParams& p, const floa
         tr.ray.dx = m[0] * ex + m[1] * ey + m[2] * ez;
         tr.ray.dy = m[4] * ex + m[5] * ey + m[6] * ez;
         tr.ray.dz = m[8] * ex + m[9] * ey + m[10] * ez;
+        fix_ray(p, m, b, sx, sy, sz, tx, ty, tz, tr);
         ray_window(tr.ray, p.D, p.H, p.W, p.S);
         if (p.t_window) apply_t_window(tr.ray, __ldg(p.t_window + bn * 2), __ldg(p.t_window + bn * 2 + 1), p.S);
         if (p.win) {
@@ -212,13 +245,13 @@ constexpr int kLayoutQuadLab = 2;  // labelled quad layout (16-bit volumes): cla
 // The eight corners of the sample's cell from the plain volume (bounds
 // checked per corner) or from the quad layouts (two vector loads).
 template <typename VT, int QUAD>
-__device__ __forceinline__ void fetch_cell(const MarchParams& p, float x, float y, float z, Cell& c) {
+__device__ __forceinline__ void fetch_cell(const MarchParams& p, const FixPos& P, Cell& c) {
     if constexpr (QUAD == kLayoutQuadLab) {
-        load_cell_quad_labeled<VT>(p.quad, p.qg, p.D, p.H, p.W, x, y, z, c);
+        load_cell_quad_labeled_fix<VT>(p.quad, p.qg, p.D, p.H, p.W, P, c);
     } else if constexpr (QUAD == kLayoutQuad) {
-        load_cell_quad<VT>(p.quad, p.qg, p.D, p.H, p.W, x, y, z, c);
+        load_cell_quad_fix<VT>(p.quad, p.qg, p.D, p.H, p.W, P, c);
     } else {
-        load_cell(reinterpret_cast<const VT*>(p.vol), p.D, p.H, p.W, x, y, z, c);
+        load_cell_fix(reinterpret_cast<const VT*>(p.vol), p.D, p.H, p.W, P, c);
     }
 }
 
@@ -253,13 +286,10 @@ __device__ __forceinline__ void fwd_body(const MarchParams& p, const int tile, c
     if (MULTI) {
         for (int c = 0; c < p.C; ++c) cacc[c * NT] = 0.f;
     }
-    for (int s = tr.s0; s < tr.s1; ++s) {
-        const float t = (float)s * p.inv_s;
-        const float x = fmaf(t, tr.ray.dx, tr.ray.p0x);
-        const float y = fmaf(t, tr.ray.dy, tr.ray.p0y);
-        const float z = fmaf(t, tr.ray.dz, tr.ray.p0z);
+    FixPos P = fix_at(tr, tr.s0);
+    for (int s = tr.s0; s < tr.s1; ++s, P = fix_add(P, tr.fd)) {
         Cell cell;
-        fetch_cell<VT, QUAD>(p, x, y, z, cell);
+        fetch_cell<VT, QUAD>(p, P, cell);
         const float val = cell_value(cell);
         acc += val;
         if (p.out_extent) {
@@ -275,7 +305,7 @@ __device__ __forceinline__ void fwd_body(const MarchParams& p, const int tile, c
             if constexpr (QUAD == kLayoutQuadLab) {
                 cls = cell.cls;
             } else {
-                cls = nearest_label(p.lab, p.lab_dtype, p.D, p.H, p.W, x, y, z);
+                cls = nearest_label_fix(p.lab, p.lab_dtype, p.D, p.H, p.W, P);
             }
             if ((unsigned)cls < (unsigned)p.C) cacc[cls * NT] += val;
         }
@@ -502,10 +532,10 @@ __device__ __forceinline__ float class_go(const MarchParams& p, int b, const Thr
 }
 
 template <bool MULTI>
-__device__ __forceinline__ float sample_go(const MarchParams& p, int b, const ThreadRay& tr, float go_ray, float x,
-                                           float y, float z) {
+__device__ __forceinline__ float sample_go(const MarchParams& p, int b, const ThreadRay& tr, float go_ray,
+                                           const FixPos& P) {
     if (!MULTI) return go_ray;
-    return class_go(p, b, tr, nearest_label(p.lab, p.lab_dtype, p.D, p.H, p.W, x, y, z));
+    return class_go(p, b, tr, nearest_label_fix(p.lab, p.lab_dtype, p.D, p.H, p.W, P));
 }
 
 // Adjoint terms of one sample whose cell is loaded.
@@ -523,15 +553,15 @@ __device__ __forceinline__ void adjoint_samples(const MarchParams& p, const floa
                                                 const Scatter& scatter) {
     if (!MULTI && go_ray == 0.f) return;  // every term is proportional to go
     int s = s0;
+    FixPos Pa = fix_at(tr, s0);
+    const FixPos fd2 = fix_add(tr.fd, tr.fd);
     if constexpr (QUAD == kLayoutQuadLab) {
         // the class of a sample arrives with its corners: fetch, then route
-        for (; s + 1 < s1; s += 2) {
+        for (; s + 1 < s1; s += 2, Pa = fix_add(Pa, fd2)) {
             const float ta = (float)s * p.inv_s, tb = (float)(s + 1) * p.inv_s;
             Cell ca, cb;
-            fetch_cell<VT, QUAD>(p, fmaf(ta, tr.ray.dx, tr.ray.p0x), fmaf(ta, tr.ray.dy, tr.ray.p0y),
-                                 fmaf(ta, tr.ray.dz, tr.ray.p0z), ca);
-            fetch_cell<VT, QUAD>(p, fmaf(tb, tr.ray.dx, tr.ray.p0x), fmaf(tb, tr.ray.dy, tr.ray.p0y),
-                                 fmaf(tb, tr.ray.dz, tr.ray.p0z), cb);
+            fetch_cell<VT, QUAD>(p, Pa, ca);
+            fetch_cell<VT, QUAD>(p, fix_add(Pa, tr.fd), cb);
             const float ga = MULTI ? class_go(p, b, tr, ca.cls) : go_ray;
             const float gb = MULTI ? class_go(p, b, tr, cb.cls) : go_ray;
             if (ga != 0.f) adjoint_accumulate<GVOL, GCAM>(m, tr, ta, ga, ca, A, scatter);
@@ -540,35 +570,29 @@ __device__ __forceinline__ void adjoint_samples(const MarchParams& p, const floa
         if (s < s1) {
             const float t = (float)s * p.inv_s;
             Cell cell;
-            fetch_cell<VT, QUAD>(p, fmaf(t, tr.ray.dx, tr.ray.p0x), fmaf(t, tr.ray.dy, tr.ray.p0y),
-                                 fmaf(t, tr.ray.dz, tr.ray.p0z), cell);
+            fetch_cell<VT, QUAD>(p, Pa, cell);
             const float gg = MULTI ? class_go(p, b, tr, cell.cls) : go_ray;
             if (gg != 0.f) adjoint_accumulate<GVOL, GCAM>(m, tr, t, gg, cell, A, scatter);
         }
         return;
     }
-    for (; s + 1 < s1; s += 2) {
+    for (; s + 1 < s1; s += 2, Pa = fix_add(Pa, fd2)) {
         const float ta = (float)s * p.inv_s, tb = (float)(s + 1) * p.inv_s;
-        const float xa = fmaf(ta, tr.ray.dx, tr.ray.p0x), xb = fmaf(tb, tr.ray.dx, tr.ray.p0x);
-        const float ya = fmaf(ta, tr.ray.dy, tr.ray.p0y), yb = fmaf(tb, tr.ray.dy, tr.ray.p0y);
-        const float za = fmaf(ta, tr.ray.dz, tr.ray.p0z), zb = fmaf(tb, tr.ray.dz, tr.ray.p0z);
-        const float ga = sample_go<MULTI>(p, b, tr, go_ray, xa, ya, za);
-        const float gb = sample_go<MULTI>(p, b, tr, go_ray, xb, yb, zb);
+        const FixPos Pb = fix_add(Pa, tr.fd);
+        const float ga = sample_go<MULTI>(p, b, tr, go_ray, Pa);
+        const float gb = sample_go<MULTI>(p, b, tr, go_ray, Pb);
         Cell ca, cb;
-        fetch_cell<VT, QUAD>(p, xa, ya, za, ca);
-        fetch_cell<VT, QUAD>(p, xb, yb, zb, cb);
+        fetch_cell<VT, QUAD>(p, Pa, ca);
+        fetch_cell<VT, QUAD>(p, Pb, cb);
         if (ga != 0.f) adjoint_accumulate<GVOL, GCAM>(m, tr, ta, ga, ca, A, scatter);
         if (gb != 0.f) adjoint_accumulate<GVOL, GCAM>(m, tr, tb, gb, cb, A, scatter);
     }
     if (s < s1) {
         const float t = (float)s * p.inv_s;
-        const float x = fmaf(t, tr.ray.dx, tr.ray.p0x);
-        const float y = fmaf(t, tr.ray.dy, tr.ray.p0y);
-        const float z = fmaf(t, tr.ray.dz, tr.ray.p0z);
-        const float gg = sample_go<MULTI>(p, b, tr, go_ray, x, y, z);
+        const float gg = sample_go<MULTI>(p, b, tr, go_ray, Pa);
         if (gg != 0.f) {
             Cell cell;
-            fetch_cell<VT, QUAD>(p, x, y, z, cell);
+            fetch_cell<VT, QUAD>(p, Pa, cell);
             adjoint_accumulate<GVOL, GCAM>(m, tr, t, gg, cell, A, scatter);
         }
     }
@@ -684,24 +708,23 @@ struct SlabCut {
     int c0, c1;
 };
 
-// Cell index of the quad scatter along one axis (the clamp and floor of
-// quad_cell), shifted by 2 into [0, dim + 2].
-__device__ __forceinline__ int cell_index_shifted(const Ray& r, int axis, float t, int dim) {
-    const float p0 = axis == 0 ? r.p0x : (axis == 1 ? r.p0y : r.p0z);
-    const float d = axis == 0 ? r.dx : (axis == 1 ? r.dy : r.dz);
-    const float x = fminf(fmaxf(fmaf(t, d, p0), -2.0f), (float)dim + 1.0f);
-    return min((int)floorf(x), dim) + 2;
+// Cell index of the quad scatter along one axis at sample s (fix_cell's
+// clamped integer part), shifted by 2 into [0, dim + 2].
+__device__ __forceinline__ int cell_index_shifted(const ThreadRay& tr, int axis, int s, int dim) {
+    const long long f0 = axis == 0 ? tr.f0.x : (axis == 1 ? tr.f0.y : tr.f0.z);
+    const long long fd = axis == 0 ? tr.fd.x : (axis == 1 ? tr.fd.y : tr.fd.z);
+    return min(max(fix_floor(f0 + (long long)s * fd), -2), dim) + 2;
 }
 
 // First s in [lo, hi) whose cell index along the cut's axis is >= c (index
 // non-decreasing in s) or < c (non-increasing); hi when there is none. The
-// index is monotonic in s, so a binary search over the exact per-sample
-// computation finds the boundary.
-__device__ __forceinline__ int slab_bound(const Ray& r, const MarchParams& p, int axis, int dim, int lo, int hi,
-                                          int c, bool increasing) {
+// index is monotonic in s (exact integer positions), so a binary search over
+// the same per-sample computation the march uses finds the boundary.
+__device__ __forceinline__ int slab_bound(const ThreadRay& tr, int axis, int dim, int lo, int hi, int c,
+                                          bool increasing) {
     while (lo < hi) {
         const int mid = lo + ((hi - lo) >> 1);
-        const int i = cell_index_shifted(r, axis, (float)mid * p.inv_s, dim);
+        const int i = cell_index_shifted(tr, axis, mid, dim);
         if (increasing ? (i >= c) : (i < c))
             hi = mid;
         else
@@ -715,16 +738,16 @@ __device__ __forceinline__ void restrict_to_slab(const MarchParams& p, ThreadRay
     Ray& r = tr.ray;
     if (r.lo >= r.hi) return;
     const int dim = cut.axis == 0 ? p.W : (cut.axis == 1 ? p.H : p.D);
-    const float d = cut.axis == 0 ? r.dx : (cut.axis == 1 ? r.dy : r.dz);
+    const long long d = cut.axis == 0 ? tr.fd.x : (cut.axis == 1 ? tr.fd.y : tr.fd.z);
     int a, e;
-    if (d > 0.f) {
-        a = slab_bound(r, p, cut.axis, dim, r.lo, r.hi, cut.c0, true);
-        e = slab_bound(r, p, cut.axis, dim, a, r.hi, cut.c1, true);
-    } else if (d < 0.f) {
-        a = slab_bound(r, p, cut.axis, dim, r.lo, r.hi, cut.c1, false);
-        e = slab_bound(r, p, cut.axis, dim, a, r.hi, cut.c0, false);
+    if (d > 0) {
+        a = slab_bound(tr, cut.axis, dim, r.lo, r.hi, cut.c0, true);
+        e = slab_bound(tr, cut.axis, dim, a, r.hi, cut.c1, true);
+    } else if (d < 0) {
+        a = slab_bound(tr, cut.axis, dim, r.lo, r.hi, cut.c1, false);
+        e = slab_bound(tr, cut.axis, dim, a, r.hi, cut.c0, false);
     } else {
-        const int i = cell_index_shifted(r, cut.axis, (float)r.lo * p.inv_s, dim);
+        const int i = cell_index_shifted(tr, cut.axis, r.lo, dim);
         const bool in = i >= cut.c0 && i < cut.c1;
         a = r.lo;
         e = in ? r.hi : r.lo;
@@ -804,8 +827,8 @@ __device__ __forceinline__ void block_box(int (&lo)[3], int (&hi)[3], int* sred,
     hi[2] = -box[5];
 }
 
-__device__ __forceinline__ int floor_clamped(float v, float lo, float hi) {
-    return (int)floorf(fminf(fmaxf(v, lo), hi));
+__device__ __forceinline__ int floor_clamped(long long v, int lo, int hi) {
+    return min(max(fix_floor(v), lo), hi);
 }
 
 // Adjoint with the volume gradient privatised per slab: the CTA's rays march
@@ -852,7 +875,6 @@ __global__ void __launch_bounds__(256, 2) raymarch_bwd_brick_kernel(const MarchP
 
     AdjAcc A;
     A.zero();
-    const float fW = (float)p.W, fH = (float)p.H, fD = (float)p.D;
     int L = L0;
     for (int sb = smin; sb < smax;) {
         const int se = min(sb + L, smax);
@@ -860,13 +882,10 @@ __global__ void __launch_bounds__(256, 2) raymarch_bwd_brick_kernel(const MarchP
         lo3[0] = lo3[1] = lo3[2] = INT_MAX;
         hi3[0] = hi3[1] = hi3[2] = -INT_MAX;
         if (a < e) {
-            const float ta = (float)a * p.inv_s, te = (float)(e - 1) * p.inv_s;
-            const int xa = floor_clamped(fmaf(ta, tr.ray.dx, tr.ray.p0x), -2.f, fW + 1.f);
-            const int xe = floor_clamped(fmaf(te, tr.ray.dx, tr.ray.p0x), -2.f, fW + 1.f);
-            const int ya = floor_clamped(fmaf(ta, tr.ray.dy, tr.ray.p0y), -2.f, fH + 1.f);
-            const int ye = floor_clamped(fmaf(te, tr.ray.dy, tr.ray.p0y), -2.f, fH + 1.f);
-            const int za = floor_clamped(fmaf(ta, tr.ray.dz, tr.ray.p0z), -2.f, fD + 1.f);
-            const int ze = floor_clamped(fmaf(te, tr.ray.dz, tr.ray.p0z), -2.f, fD + 1.f);
+            const FixPos Pa = fix_at(tr, a), Pe = fix_at(tr, e - 1);
+            const int xa = floor_clamped(Pa.x, -2, p.W), xe = floor_clamped(Pe.x, -2, p.W);
+            const int ya = floor_clamped(Pa.y, -2, p.H), ye = floor_clamped(Pe.y, -2, p.H);
+            const int za = floor_clamped(Pa.z, -2, p.D), ze = floor_clamped(Pe.z, -2, p.D);
             // corners span [floor, floor + 1], clipped to the volume
             int l0 = max(min(xa, xe), 0), h0 = min(max(xa, xe) + 1, p.W - 1);
             int l1 = max(min(ya, ye), 0), h1 = min(max(ya, ye) + 1, p.H - 1);

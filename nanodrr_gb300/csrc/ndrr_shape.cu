@@ -15,6 +15,7 @@ MarchParams make_params(const ndrr_raymarch_args& a, const LaunchShape& ls) {
     p.lab_dtype = a.lab_dtype;
     p.C = a.n_classes;
     p.M = a.M;
+    p.M_lo = a.M_lo;
     p.src = a.src;
     p.tgt = a.tgt;
     p.step = a.step;

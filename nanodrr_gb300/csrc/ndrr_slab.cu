@@ -137,8 +137,8 @@ __global__ void __launch_bounds__(512) slab_plan_kernel(const MarchParams p, con
         init_thread_ray(p, m, b, n, tr);
         if (n >= 0 && tr.ray.lo < tr.ray.hi) {
             const int dim = axis == 0 ? p.W : (axis == 1 ? p.H : p.D);
-            const int i0 = cell_index_shifted(tr.ray, axis, (float)tr.ray.lo * p.inv_s, dim);
-            const int i1 = cell_index_shifted(tr.ray, axis, (float)(tr.ray.hi - 1) * p.inv_s, dim);
+            const int i0 = cell_index_shifted(tr, axis, tr.ray.lo, dim);
+            const int i1 = cell_index_shifted(tr, axis, tr.ray.hi - 1, dim);
             atomicMin(&red[0], min(i0, i1) / s.Z[axis]);
             atomicMax(&red[1], max(i0, i1) / s.Z[axis]);
         }

@@ -113,6 +113,15 @@ def _base_args(vol, lab, M, src, tgt, step, n_samples, n_classes, width) -> _ffi
     return a
 
 
+def _set_M_lo(a: _ffi.RaymarchArgs, M_lo: torch.Tensor | None, M: torch.Tensor) -> None:
+    """Point the arguments at the affine's low parts (kept alive by the caller)."""
+    if M_lo is None or M_lo.numel() == 0:
+        return
+    if tuple(M_lo.shape) != tuple(M.shape) or M_lo.dtype != torch.float32 or not M_lo.is_contiguous():
+        raise ValueError("M_lo must be a contiguous float32 tensor shaped like M")
+    a.M_lo = M_lo.data_ptr()
+
+
 def _apply_skip(a: _ffi.RaymarchArgs, skip, vol: torch.Tensor) -> None:
     """Fill the empty-space fields of the C-ABI arguments from an EmptySpace."""
     if skip is None or skip.mode == _ffi.NDRR_SKIP_NONE:
@@ -305,6 +314,7 @@ def raymarch_forward(
     windows: torch.Tensor | None = None,
     texture: TextureVolume | None = None,
     fwd_mode: int = 0,
+    M_lo: torch.Tensor | None = None,
 ) -> tuple[torch.Tensor, torch.Tensor | None]:
     """Launch the forward kernel; returns (out [B, C, N], total [B, N] or None).
 
@@ -315,7 +325,8 @@ def raymarch_forward(
     `quad` the volume's quad-layout copy (`quad_volume`), read instead of
     `vol` when given. The learned proposal, and an occupancy skip built with
     `fused=False`, are applied through per-ray windows (`skip_windows`);
-    `windows` passes windows computed earlier. `fwd_mode` 1 selects the
+    `windows` passes windows computed earlier. `M_lo` the low parts of the
+    affine (M + M_lo; see ndrr_raymarch_args). `fwd_mode` 1 selects the
     TMA-staged forward (a measured variant: f32, one channel, no skipping)
     and `texture` the texture-filtered one (`TextureVolume`)."""
     _check_inputs(vol, lab, M, src, tgt, step, n_samples, n_classes)
@@ -331,6 +342,7 @@ def raymarch_forward(
     out = torch.empty(B, n_classes, N, device=vol.device, dtype=odt)
     total = torch.empty(B, N, device=vol.device, dtype=odt) if with_total else None
     a = _base_args(vol, lab, M, src, tgt, step, n_samples, n_classes, width)
+    _set_M_lo(a, M_lo, M)
     a.out = _ptr(out)
     a.out_dtype = ndrr_dtype(out)
     a.out_total = _ptr(total)
@@ -387,6 +399,7 @@ def raymarch_backward(
     skip=None,
     quad: torch.Tensor | None = None,
     windows: torch.Tensor | None = None,
+    M_lo: torch.Tensor | None = None,
 ):
     """Launch the adjoint; returns (gvol, gM, gsrc, gtgt, gstep) in float32.
 
@@ -436,6 +449,7 @@ def raymarch_backward(
     else:
         gsrc = gtgt = gstep = empty
     a = _base_args(vol, lab, M, src, tgt, step, n_samples, n_classes, width)
+    _set_M_lo(a, M_lo, M)
     a.go = _ptr(go)
     a.go_dtype = ndrr_dtype(go)
     a.need_gvol = int(need_gvol)
@@ -598,6 +612,7 @@ def fused_raymarch_ex(
     quad: torch.Tensor,
     lab: torch.Tensor,
     M: torch.Tensor,
+    M_lo: torch.Tensor,
     src: torch.Tensor,
     tgt: torch.Tensor,
     step: torch.Tensor,
@@ -615,13 +630,15 @@ def fused_raymarch_ex(
     """Returns (out [B, C, N], windows): with `windows_ahead` and a skip, the
     per-ray sample windows [B, N, 2] int32 the forward used, which the
     pose/camera adjoint reuses; otherwise an empty int32 tensor. `slab_mib`
-    is the adjoint's slab size (0 = default), passed through to it."""
-    return fused_raymarch_ex_forward(vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid,
+    is the adjoint's slab size (0 = default), passed through to it. `M_lo`
+    holds the low parts of the affine (M + M_lo, see ndrr_raymarch_args) or
+    is empty."""
+    return fused_raymarch_ex_forward(vol, quad, lab, M, M_lo, src, tgt, step, n_samples, n_classes, width, occ_grid,
                                      occ_cell, proposal, skip_mode, margin, windows_ahead, slab_mib)
 
 
-def fused_raymarch_ex_forward(vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell,
-                              proposal, skip_mode, margin, windows_ahead, slab_mib):
+def fused_raymarch_ex_forward(vol, quad, lab, M, M_lo, src, tgt, step, n_samples, n_classes, width, occ_grid,
+                              occ_cell, proposal, skip_mode, margin, windows_ahead, slab_mib):
     """The forward of `fused_raymarch_ex` without the op dispatch (the caller
     uses it when no gradient is recorded and nothing is being traced)."""
     skip = _skip_of(vol, occ_grid, occ_cell, proposal, skip_mode, margin)
@@ -630,14 +647,14 @@ def fused_raymarch_ex_forward(vol, quad, lab, M, src, tgt, step, n_samples, n_cl
         windows = skip_windows(vol, M, src, tgt, step, n_samples, width, skip)
         skip = None
     out, _ = raymarch_forward(vol, lab, M, src, tgt, step, n_samples, n_classes, width, skip=skip, quad=quad,
-                              windows=windows)
+                              windows=windows, M_lo=M_lo)
     if windows is None:
         windows = torch.empty(0, device=vol.device, dtype=torch.int32)
     return out, windows
 
 
 @fused_raymarch_ex.register_fake
-def _(vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell, proposal, skip_mode,
+def _(vol, quad, lab, M, M_lo, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell, proposal, skip_mode,
       margin, windows_ahead, slab_mib):
     B, N, _ = tgt.shape
     out = torch.empty(B, n_classes, N, device=vol.device, dtype=vol.dtype)
@@ -653,6 +670,7 @@ def fused_raymarch_ex_bwd(
     quad: torch.Tensor,
     lab: torch.Tensor,
     M: torch.Tensor,
+    M_lo: torch.Tensor,
     src: torch.Tensor,
     tgt: torch.Tensor,
     step: torch.Tensor,
@@ -680,12 +698,12 @@ def fused_raymarch_ex_bwd(
         skip, win = _skip_of(vol, occ_grid, occ_cell, proposal, skip_mode, margin), None
     return raymarch_backward(
         go, vol, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam, skip=skip, quad=quad,
-        windows=win, slab_mib=slab_mib,
+        windows=win, slab_mib=slab_mib, M_lo=M_lo,
     )
 
 
 @fused_raymarch_ex_bwd.register_fake
-def _(go, vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam, *rest):
+def _(go, vol, quad, lab, M, M_lo, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam, *rest):
     B, N, _ = tgt.shape
     gM = torch.empty(B, 3, 4, device=M.device, dtype=torch.float32)
     empty = gM.new_empty(0)
@@ -697,19 +715,19 @@ def _(go, vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, need_g
 
 
 def _ex_setup_context(ctx, inputs, output):
-    (vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell, proposal, mode,
+    (vol, quad, lab, M, M_lo, src, tgt, step, n_samples, n_classes, width, occ_grid, occ_cell, proposal, mode,
      margin, windows_ahead, slab_mib) = inputs
-    ctx.save_for_backward(vol, quad, lab, M.contiguous(), src, tgt, step, occ_grid, proposal, output[1])
+    ctx.save_for_backward(vol, quad, lab, M.contiguous(), M_lo, src, tgt, step, occ_grid, proposal, output[1])
     ctx.args = (n_samples, n_classes, width, occ_cell, mode, margin, slab_mib)
 
 
 def _ex_backward(ctx, go, _gwin):
-    vol, quad, lab, M, src, tgt, step, occ_grid, proposal, windows = ctx.saved_tensors
+    vol, quad, lab, M, M_lo, src, tgt, step, occ_grid, proposal, windows = ctx.saved_tensors
     n_samples, n_classes, width, occ_cell, mode, margin, slab_mib = ctx.args
     need_gvol = ctx.needs_input_grad[0]
-    need_gcam = any(ctx.needs_input_grad[i] for i in (4, 5, 6))
+    need_gcam = any(ctx.needs_input_grad[i] for i in (5, 6, 7))
     gvol, gM, gsrc, gtgt, gstep = fused_raymarch_ex_bwd(
-        go, vol, quad, lab, M, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam,
+        go, vol, quad, lab, M, M_lo, src, tgt, step, n_samples, n_classes, width, need_gvol, need_gcam,
         occ_grid, occ_cell, proposal, mode, margin, windows, slab_mib,
     )
     return (
@@ -717,6 +735,7 @@ def _ex_backward(ctx, go, _gwin):
         None,  # quad: a derived copy of vol
         None,  # lab
         gM.to(M.dtype),
+        None,  # M_lo: a rounding correction of M, not differentiated
         gsrc.to(src.dtype) if need_gcam else None,
         gtgt.to(tgt.dtype) if need_gcam else None,
         gstep.to(step.dtype) if need_gcam else None,

@@ -18,12 +18,10 @@ import weakref
 import torch
 
 from .raymarch import (
-    fused_raymarch,
     fused_raymarch_ex,
     fused_raymarch_ex_forward,
     quad_volume,
     quad_volume_labeled,
-    raymarch_forward,
 )
 from .subject import Subject
 
@@ -97,17 +95,26 @@ def compact_label(subject: Subject) -> torch.Tensor:
 
 
 def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) -> torch.Tensor:
-    """Adapter from the render call to the `nanodrr_gb300::fused_raymarch` op."""
+    """Adapter from the render call to the `nanodrr_gb300::fused_raymarch_ex` op (the
+    reference's `fused_raymarch` contract plus the layout, skip and the
+    affine's low parts)."""
     C = subject.n_classes
     img = subject.image
     # A reshape of the [1, 1, D, H, W] image back-propagates as a view; an
     # index ([0, 0]) would allocate and zero a volume-sized gradient per level.
     vol = (img.reshape(img.shape[-3:]) if img.shape[:2] == (1, 1) else img[0, 0]).contiguous()
     lab = compact_label(subject) if C > 1 else vol
-    M = _affine_product(subject.world_to_voxel.float()[:3], rt_inv.float())
+    # The camera -> voxel affine in float64 from the float32 (or float64)
+    # inputs, handed to the kernels as float32 M plus its rounding error M_lo:
+    # they form sample positions from M + M_lo in float-float and carry them
+    # in fixed point (see ndrr_raymarch_args.M_lo).
+    M64 = _affine_product(subject.world_to_voxel.double()[:3], rt_inv.double())
+    M = M64.float()
+    M_lo = (M64.detach() - M.detach().double()).float()
     B = max(M.shape[0], tgt.shape[0])
     if M.shape[0] != B:
         M = M.expand(B, -1, -1)
+        M_lo = M_lo.expand(B, -1, -1)
     if not fused_supported(subject, B, height * width):
         raise ValueError("inputs exceed the CUDA kernel's limits (int32 indexing)")
     args = (
@@ -132,19 +139,16 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
     # the custom op's dispatch (tens of microseconds of host time per call).
     direct = not compiling and not (torch.is_grad_enabled() and any(
         t.requires_grad for t in (args[0], args[2], args[3], args[4], args[5])))
-    if skip is None and layout == "plain":
-        out = raymarch_forward(*args)[0] if direct else fused_raymarch(*args)
+    quad = cached_quad(subject, vol, lab, C) if layout == "quad" else vol.new_empty(0, dtype=torch.uint8)
+    empty = vol.new_empty(0, dtype=torch.uint8)
+    if skip is not None:
+        sk = (skip.grid.grid, skip.grid.cell, skip.packed, int(skip.mode), float(skip.margin),
+              not getattr(skip, "fused", True))
     else:
-        quad = cached_quad(subject, vol, lab, C) if layout == "quad" else vol.new_empty(0, dtype=torch.uint8)
-        empty = vol.new_empty(0, dtype=torch.uint8)
-        if skip is not None:
-            sk = (skip.grid.grid, skip.grid.cell, skip.packed, int(skip.mode), float(skip.margin),
-                  not getattr(skip, "fused", True))
-        else:
-            sk = (empty, 0, empty, 0, 0.0, False)
-        slab_mib = int(getattr(subject, "slab_mib", 0))
-        op = fused_raymarch_ex_forward if direct else fused_raymarch_ex
-        out = op(args[0], quad, *args[1:], *sk, slab_mib)[0]
+        sk = (empty, 0, empty, 0, 0.0, False)
+    slab_mib = int(getattr(subject, "slab_mib", 0))
+    op = fused_raymarch_ex_forward if direct else fused_raymarch_ex
+    out = op(args[0], quad, args[1], args[2], M_lo.contiguous(), *args[3:], *sk, slab_mib)[0]
     return out.reshape(B, C, height, width)
 
 

@@ -42,7 +42,7 @@ def test_abi_version_and_struct_layout(lib):
     assert lib.ndrr_abi_version() == _ffi.ABI_VERSION
     assert b"sm_103a" in lib.ndrr_build_info()
     # 64-bit layout of ndrr_raymarch_args as declared in the header
-    assert ctypes.sizeof(_ffi.RaymarchArgs) == 352
+    assert ctypes.sizeof(_ffi.RaymarchArgs) == 360
     assert ctypes.sizeof(_ffi.OccupancyArgs) == 56
 
 

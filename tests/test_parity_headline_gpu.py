@@ -15,7 +15,8 @@ analytic backward) on the same float32 inputs cast to float64:
   - the plain march, the occupancy skip and the learned proposal, the skips
     also through their pose-only adjoint (sample windows);
   - the registration step's se(3) 6-vector gradient (pose kernel, render,
-    NCC kernels, backward) against float64 autograd of the same loss;
+    NCC kernels, backward) against float64 autograd of the same loss at the
+    same (float32) pose;
   - the per-label render of the 512 x 512 x 400 volume with 8 classes, f32
     and bf16 (the reference's channel-sum rule, tests/drr/test_fused.py:
     56-65: channel sum within the tolerance, fewer than 0.1 % of rays with a
@@ -196,7 +197,11 @@ def test_headline_registration_se3_gradient_within_1e3_of_fp64(headline):
 
     params = torch.cat([reg._rot, reg._xyz], dim=1).detach().double().cpu().requires_grad_(True)
     rt64, piv, piv_inv = (t.detach().double().cpu() for t in (reg.rt_inv, reg.pivot, reg.pivot_inv))
-    pose = rt64 @ piv @ convert(params[:, :3], params[:, 3:], "so3_log") @ piv_inv
+    exact = rt64 @ piv @ convert(params[:, :3], params[:, 3:], "so3_log") @ piv_inv
+    # identical inputs: the float32 pose the renderer received (the pose
+    # kernel's output), differentiated through the exact composition — the
+    # loss's gradient moves by ~1e-3 when only the pose is rounded to float32
+    pose = exact + (reg.pose.detach().double().cpu() - exact).detach()
     tgt64 = _make_tgt(k_inv.double().cpu(), sdd.double().cpu(), det, det, "cpu", torch.float64)
     src64 = _make_src(False, tgt64, sdd.double().cpu())
     vol64 = sub._image_hu.detach()[0, 0].double().cpu()
