@@ -321,6 +321,130 @@ __device__ __forceinline__ void cell_grad(const Cell& c, float& gx, float& gy, f
     gz = fmaf(z11, c.fy, __fmul_rn(z00, wy0));
 }
 
+// ---------------------------------------------- float positions (forward)
+// The forward evaluates sample positions in float32, as p0 + t * d with one
+// rounding (its images are within 1e-6 of the float64 oracle at 512^3); the
+// adjoint, whose gradients jump at cell faces, uses the fixed-point versions
+// below. Positions are clamped to [-2, dim + 1] first: beyond that every
+// corner is outside the volume either way, and the clamp keeps the float ->
+// int conversion in range for any input.
+template <typename VT>
+__device__ __forceinline__ void load_cell(const VT* __restrict__ vol, int D, int H, int W, float x, float y,
+                                          float z, Cell& c) {
+    // Positions are clamped to [-2, dim + 1] first: beyond that every corner
+    // is outside the volume either way, and the clamp keeps the float -> int
+    // conversion in range for any input.
+    x = fminf(fmaxf(x, -2.0f), (float)W + 1.0f);
+    y = fminf(fmaxf(y, -2.0f), (float)H + 1.0f);
+    z = fminf(fmaxf(z, -2.0f), (float)D + 1.0f);
+    const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+    c.fx = x - xf;
+    c.fy = y - yf;
+    c.fz = z - zf;
+    const int ix = (int)xf, iy = (int)yf, iz = (int)zf;
+    c.ix = ix;
+    c.iy = iy;
+    c.iz = iz;
+    const int HW = H * W;
+    const int base = (iz * H + iy) * W + ix;
+    if ((unsigned)ix < (unsigned)(W - 1) && (unsigned)iy < (unsigned)(H - 1) && (unsigned)iz < (unsigned)(D - 1)) {
+        c.v000 = ld_vox(vol, base);
+        c.v001 = ld_vox(vol, base + 1);
+        c.v010 = ld_vox(vol, base + W);
+        c.v011 = ld_vox(vol, base + W + 1);
+        c.v100 = ld_vox(vol, base + HW);
+        c.v101 = ld_vox(vol, base + HW + 1);
+        c.v110 = ld_vox(vol, base + HW + W);
+        c.v111 = ld_vox(vol, base + HW + W + 1);
+    } else {
+        const bool x0 = (unsigned)ix < (unsigned)W, x1 = (unsigned)(ix + 1) < (unsigned)W;
+        const bool y0 = (unsigned)iy < (unsigned)H, y1 = (unsigned)(iy + 1) < (unsigned)H;
+        const bool z0 = (unsigned)iz < (unsigned)D, z1 = (unsigned)(iz + 1) < (unsigned)D;
+        c.v000 = (z0 && y0 && x0) ? ld_vox(vol, base) : 0.f;
+        c.v001 = (z0 && y0 && x1) ? ld_vox(vol, base + 1) : 0.f;
+        c.v010 = (z0 && y1 && x0) ? ld_vox(vol, base + W) : 0.f;
+        c.v011 = (z0 && y1 && x1) ? ld_vox(vol, base + W + 1) : 0.f;
+        c.v100 = (z1 && y0 && x0) ? ld_vox(vol, base + HW) : 0.f;
+        c.v101 = (z1 && y0 && x1) ? ld_vox(vol, base + HW + 1) : 0.f;
+        c.v110 = (z1 && y1 && x0) ? ld_vox(vol, base + HW + W) : 0.f;
+        c.v111 = (z1 && y1 && x1) ? ld_vox(vol, base + HW + W + 1) : 0.f;
+    }
+}
+
+// Quad index of the cell whose lower corner is the floor of (x, y, z),
+// clamped into the padded extent, plus the fractional offsets and the cell's
+// (clamped) corner indices for the gradient scatter.
+__device__ __forceinline__ int quad_cell(const QuadGeom& g, int D, int H, int W, float x, float y, float z,
+                                         Cell& c) {
+    x = fminf(fmaxf(x, -2.0f), (float)W + 1.0f);
+    y = fminf(fmaxf(y, -2.0f), (float)H + 1.0f);
+    z = fminf(fmaxf(z, -2.0f), (float)D + 1.0f);
+    const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+    c.fx = x - xf;
+    c.fy = y - yf;
+    c.fz = z - zf;
+    c.ix = min((int)xf, W);
+    c.iy = min((int)yf, H);
+    c.iz = min((int)zf, D);
+    return ((c.iz + 2) * g.qy + (c.iy + 2)) * g.qx + (c.ix + 2);
+}
+
+template <typename VT>
+__device__ __forceinline__ void load_cell_quad(const void* __restrict__ quad, const QuadGeom& g, int D, int H,
+                                               int W, float x, float y, float z, Cell& c) {
+    const int qi = quad_cell(g, D, H, W, x, y, z, c);
+    using Q = typename QuadOf<VT>::T;
+    const Q* __restrict__ qp = reinterpret_cast<const Q*>(quad);
+    const Q q0 = __ldg(qp + qi);
+    const Q q1 = __ldg(qp + qi + g.plane);
+    if constexpr (std::is_same<VT, float>::value) {
+        unpack_quad(q0, c.v000, c.v001, c.v010, c.v011);
+        unpack_quad(q1, c.v100, c.v101, c.v110, c.v111);
+    } else if constexpr (std::is_same<VT, __nv_bfloat16>::value) {
+        unpack_quad_bf16(q0, c.v000, c.v001, c.v010, c.v011);
+        unpack_quad_bf16(q1, c.v100, c.v101, c.v110, c.v111);
+    } else {
+        unpack_quad_f16(q0, c.v000, c.v001, c.v010, c.v011);
+        unpack_quad_f16(q1, c.v100, c.v101, c.v110, c.v111);
+    }
+}
+
+// Labelled quad at a float position (see load_cell_quad_labeled_fix).
+template <typename VT>
+__device__ __forceinline__ void load_cell_quad_labeled(const void* __restrict__ quad, const QuadGeom& g, int D, int H,
+                                                       int W, float x, float y, float z, Cell& c) {
+    const int qi = quad_cell(g, D, H, W, x, y, z, c);
+    const uint4* __restrict__ qp = reinterpret_cast<const uint4*>(quad);
+    const uint4 q0 = __ldg(qp + qi);
+    const uint4 q1 = __ldg(qp + qi + g.plane);
+    if constexpr (std::is_same<VT, __nv_bfloat16>::value) {
+        unpack_quad_bf16(make_uint2(q0.x, q0.y), c.v000, c.v001, c.v010, c.v011);
+        unpack_quad_bf16(make_uint2(q1.x, q1.y), c.v100, c.v101, c.v110, c.v111);
+    } else {
+        unpack_quad_f16(make_uint2(q0.x, q0.y), c.v000, c.v001, c.v010, c.v011);
+        unpack_quad_f16(make_uint2(q1.x, q1.y), c.v100, c.v101, c.v110, c.v111);
+    }
+    const float xc = fminf(fmaxf(x, -2.0f), (float)W + 1.0f);
+    const float yc = fminf(fmaxf(y, -2.0f), (float)H + 1.0f);
+    const float zc = fminf(fmaxf(z, -2.0f), (float)D + 1.0f);
+    const int ox = (int)rintf(xc) - c.ix, oy = (int)rintf(yc) - c.iy, oz = (int)rintf(zc) - c.iz;
+    const unsigned labels = oz ? q1.z : q0.z;
+    c.cls = (int)((labels >> (8 * (ox + 2 * oy))) & 0xffu);
+}
+
+// Nearest-voxel label at (x, y, z); ties round to even like grid_sample's
+// nearest mode. Out-of-volume positions read label 0 (zero padding).
+__device__ __forceinline__ int nearest_label(const void* __restrict__ lab, int lab_dtype, int D, int H, int W,
+                                             float x, float y, float z) {
+    x = fminf(fmaxf(x, -2.0f), (float)W + 1.0f);
+    y = fminf(fmaxf(y, -2.0f), (float)H + 1.0f);
+    z = fminf(fmaxf(z, -2.0f), (float)D + 1.0f);
+    const int rx = (int)rintf(x), ry = (int)rintf(y), rz = (int)rintf(z);
+    if ((unsigned)rx < (unsigned)W && (unsigned)ry < (unsigned)H && (unsigned)rz < (unsigned)D)
+        return ld_label(lab, lab_dtype, (rz * H + ry) * W + rx);
+    return 0;
+}
+
 // Cell of a fixed-point position: the integer parts clamped into [-2, dim]
 // (a cell there has every corner outside the volume, so the clamp changes no
 // value or gradient, and it keeps quad indices inside the padded extent) and

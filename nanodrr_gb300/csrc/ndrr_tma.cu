@@ -103,19 +103,16 @@ __device__ __forceinline__ void ray_chunk_box(const ThreadRay& tr, const MarchPa
     v[0] = v[1] = v[2] = INT_MAX;
     v[3] = v[4] = v[5] = INT_MAX;  // negated maxima
     if (a >= e) return;
-    (void)p;
-    // positions are monotone along the ray, so the chunk's two end samples
-    // bound every sample's cell
-    const FixPos Pa = fix_at(tr, a), Pe = fix_at(tr, e - 1);
-    const int xa = fix_floor(Pa.x), xe = fix_floor(Pe.x);
-    const int ya = fix_floor(Pa.y), ye = fix_floor(Pe.y);
-    const int za = fix_floor(Pa.z), ze = fix_floor(Pe.z);
-    v[0] = min(xa, xe);
-    v[1] = min(ya, ye);
-    v[2] = min(za, ze);
-    v[3] = -(max(xa, xe) + 1);  // the +1 corner
-    v[4] = -(max(ya, ye) + 1);
-    v[5] = -(max(za, ze) + 1);
+    const float ta = (float)a * p.inv_s, te = (float)(e - 1) * p.inv_s;
+    const float xa = floorf(fmaf(ta, tr.ray.dx, tr.ray.p0x)), xe = floorf(fmaf(te, tr.ray.dx, tr.ray.p0x));
+    const float ya = floorf(fmaf(ta, tr.ray.dy, tr.ray.p0y)), ye = floorf(fmaf(te, tr.ray.dy, tr.ray.p0y));
+    const float za = floorf(fmaf(ta, tr.ray.dz, tr.ray.p0z)), ze = floorf(fmaf(te, tr.ray.dz, tr.ray.p0z));
+    v[0] = (int)fminf(xa, xe);
+    v[1] = (int)fminf(ya, ye);
+    v[2] = (int)fminf(za, ze);
+    v[3] = -((int)fmaxf(xa, xe) + 1);  // the +1 corner
+    v[4] = -((int)fmaxf(ya, ye) + 1);
+    v[5] = -((int)fmaxf(za, ze) + 1);
 }
 
 __global__ void __launch_bounds__(kTRays) raymarch_fwd_tma_kernel(const MarchParams p,
@@ -203,17 +200,19 @@ __global__ void __launch_bounds__(kTRays) raymarch_fwd_tma_kernel(const MarchPar
         }
         const int a = max(lo, c0), e = min(hi, c1);
         if (!failed) {
-            FixPos P = fix_at(tr, a);
-            for (int s = a; s < e; ++s, P = fix_add(P, tr.fd)) {
+            for (int s = a; s < e; ++s) {
+                // the forward's float positions, so the image is bitwise its
+                const float t = (float)s * p.inv_s;
+                const float x = fmaf(t, tr.ray.dx, tr.ray.p0x);
+                const float y = fmaf(t, tr.ray.dy, tr.ray.p0y);
+                const float z = fmaf(t, tr.ray.dz, tr.ray.p0z);
                 Cell c;
                 if (staged) {
-                    // the same cell and fractions as fix_cell (unclamped:
-                    // the staged box covers the chunk, zero-filled outside
-                    // the volume)
-                    c.fx = fix_frac(P.x);
-                    c.fy = fix_frac(P.y);
-                    c.fz = fix_frac(P.z);
-                    const int lx = fix_floor(P.x) - ox, ly = fix_floor(P.y) - oy, lz = fix_floor(P.z) - oz;
+                    const float xf = floorf(x), yf = floorf(y), zf = floorf(z);
+                    c.fx = x - xf;
+                    c.fy = y - yf;
+                    c.fz = z - zf;
+                    const int lx = (int)xf - ox, ly = (int)yf - oy, lz = (int)zf - oz;
                     const float* bx = sh.box[stage] + (lz * kTBY + ly) * kTBX + lx;
                     c.v000 = bx[0];
                     c.v001 = bx[1];
@@ -224,7 +223,7 @@ __global__ void __launch_bounds__(kTRays) raymarch_fwd_tma_kernel(const MarchPar
                     c.v110 = bx[kTBX * kTBY + kTBX];
                     c.v111 = bx[kTBX * kTBY + kTBX + 1];
                 } else {
-                    load_cell_fix(reinterpret_cast<const float*>(p.vol), p.D, p.H, p.W, P, c);
+                    load_cell(reinterpret_cast<const float*>(p.vol), p.D, p.H, p.W, x, y, z, c);
                 }
                 acc += cell_value(c);
             }
