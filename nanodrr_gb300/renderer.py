@@ -104,17 +104,23 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
     # index ([0, 0]) would allocate and zero a volume-sized gradient per level.
     vol = (img.reshape(img.shape[-3:]) if img.shape[:2] == (1, 1) else img[0, 0]).contiguous()
     lab = compact_label(subject) if C > 1 else vol
-    # The camera -> voxel affine in float64 from the float32 (or float64)
-    # inputs, handed to the kernels as float32 M plus its rounding error M_lo:
-    # they form sample positions from M + M_lo in float-float and carry them
-    # in fixed point (see ndrr_raymarch_args.M_lo).
-    M64 = _affine_product(subject.world_to_voxel.double()[:3], rt_inv.double())
-    M = M64.float()
-    M_lo = (M64.detach() - M.detach().double()).float()
+    M = _affine_product(subject.world_to_voxel.float()[:3], rt_inv.float())
+    # With a gradient recorded, the adjoint forms sample positions from M +
+    # M_lo in float-float and carries them in fixed point
+    # (ndrr_raymarch_args.M_lo): M_lo is the float32 product's error against
+    # the float64 affine of the same inputs. The forward reads float32 M only,
+    # so a call without a gradient skips the float64 product.
+    grad = torch.is_grad_enabled() and any(t.requires_grad for t in (vol, rt_inv, src, tgt, step_size))
+    if grad:
+        M64 = _affine_product(subject.world_to_voxel.detach().double()[:3], rt_inv.detach().double())
+        M_lo = (M64 - M.detach().double()).float()
+    else:
+        M_lo = M.new_empty(0)
     B = max(M.shape[0], tgt.shape[0])
     if M.shape[0] != B:
         M = M.expand(B, -1, -1)
-        M_lo = M_lo.expand(B, -1, -1)
+        if grad:
+            M_lo = M_lo.expand(B, -1, -1)
     if not fused_supported(subject, B, height * width):
         raise ValueError("inputs exceed the CUDA kernel's limits (int32 indexing)")
     args = (
@@ -137,8 +143,7 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
     layout = "plain" if compiling else getattr(subject, "layout", "quad")
     # Without a recorded gradient the forward is called directly, skipping
     # the custom op's dispatch (tens of microseconds of host time per call).
-    direct = not compiling and not (torch.is_grad_enabled() and any(
-        t.requires_grad for t in (args[0], args[2], args[3], args[4], args[5])))
+    direct = not compiling and not grad
     quad = cached_quad(subject, vol, lab, C) if layout == "quad" else vol.new_empty(0, dtype=torch.uint8)
     empty = vol.new_empty(0, dtype=torch.uint8)
     if skip is not None:
