@@ -11,11 +11,6 @@ namespace ndrr {
 template <typename VT, bool MULTI, bool GCAM, int LAYOUT>
 static cudaError_t bwd_quad_skip(const MarchParams& p, int skip, unsigned grid, unsigned block, size_t smem,
                                  cudaStream_t st) {
-    if constexpr (!MULTI && !GCAM && LAYOUT == kLayoutQuad) {
-        if (skip == NDRR_SKIP_OCCUPANCY)
-            return launch_kernel(raymarch_bwd_pose_kernel<VT, 1, LAYOUT>, grid, block, smem, st, p);
-        return launch_kernel(raymarch_bwd_pose_kernel<VT, 0, LAYOUT>, grid, block, smem, st, p);
-    }
     if (skip == NDRR_SKIP_OCCUPANCY)
         return launch_kernel(raymarch_bwd_kernel<VT, MULTI, false, GCAM, 1, LAYOUT>, grid, block, smem, st, p);
     return launch_kernel(raymarch_bwd_kernel<VT, MULTI, false, GCAM, 0, LAYOUT>, grid, block, smem, st, p);
