@@ -757,9 +757,12 @@ def _rel_maxabs(a, b):
 def per_label_forward(dev, steps=5):
     """Per-label forward on the 512 x 512 x 400 phantom (0.8 x 0.8 x 1.0 mm),
     8 label channels plus the total, 32 poses, 256^2 detector at 1.2 mm, 800
-    samples/ray; the volume as float32 and as bf16 (quad layout, uint8 labels)."""
+    samples/ray; the volume as float32 (quad layout, uint8 label gathers) and
+    as bf16 (the labelled quad layout that render() uses for it: classes in
+    the corner loads), the bf16 volume also with label gathers, and the
+    one-channel forward of the same rays for scale."""
     from nanodrr_gb300 import phantom
-    from nanodrr_gb300.raymarch import quad_volume, raymarch_forward
+    from nanodrr_gb300.raymarch import quad_volume, quad_volume_labeled, raymarch_forward
     from nanodrr_gb300.renderer import compact_label
 
     B, det, S, C = 32, 256, 800, 8
@@ -774,17 +777,22 @@ def per_label_forward(dev, steps=5):
     res = {"workload": "512x512x400 phantom, 8 labels + total, 32 poses, 256^2, 800 samples, forward",
            "l2": "inputs larger than L2"}
     outs = {}
-    for name, v in vols.items():
-        q = quad_volume(v)
+    cases = (("f32", vols["f32"], False), ("bf16", vols["bf16"], True), ("bf16_label_gathers", vols["bf16"], False))
+    for name, v, labelled in cases:
+        q = quad_volume_labeled(v, lab, C) if labelled else quad_volume(v)
         fn = lambda: raymarch_forward(v, lab, M, src, tgt, step, S, C, det, with_total=True, quad=q)  # noqa: E731
         ms = _event_ms(fn, steps)
         outs[name] = fn()
         res[name] = {"ms": round(ms, 3), "frames_per_s": round(B / ms * 1e3, 1)}
         del q
+    q = quad_volume(vols["f32"])
+    one = lambda: raymarch_forward(vols["f32"], vols["f32"], M, src, tgt, step, S, 1, det, quad=q)  # noqa: E731
+    res["one_channel_f32_ms"] = round(_event_ms(one, steps), 3)
     res["bf16_vs_f32_rel_maxabs"] = {
         "channels": round(_rel_maxabs(outs["bf16"][0], outs["f32"][0]), 5),
         "total": round(_rel_maxabs(outs["bf16"][1], outs["f32"][1]), 5),
     }
+    res["labelled_quad_equals_label_gathers"] = bool(torch.equal(outs["bf16"][0], outs["bf16_label_gathers"][0]))
     return res
 
 
