@@ -389,17 +389,22 @@ def test_quad_layout_equals_plain_layout(dtype, C):
     assert rel_maxabs(gq[0], gp[0]) < 1e-5
 
 
-def test_render_uses_quad_layout_and_plain_on_request(random32):
+def test_render_layout_choice_and_request(random32):
+    """One pose without a gradient reads the plain volume (the quad copy's 4x
+    bytes are not reused by other poses), several poses read the quad copy,
+    and `subject.layout` overrides either; the images are the same."""
     g = random32
     sub = subject_from_arrays(g["vol"], None, g["voxel_to_world"], 1)
     k_inv, rt, sdd, H, W = rays_for(g)
-    out_q = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=200)
-    assert getattr(sub, "_ndrr_quad_cache", None) is not None
-    sub.layout = "plain"
     out_p = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=200)
+    assert getattr(sub, "_ndrr_quad_cache", None) is None
+    out_q2 = nd.render(sub, k_inv, rt.expand(2, -1, -1), sdd, H, W, n_samples=200)
+    assert getattr(sub, "_ndrr_quad_cache", None) is not None
+    assert torch.equal(out_q2[:1], out_p) and torch.equal(out_q2[1:], out_p)
+    sub.layout = "quad"
+    out_q = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=200)
     assert torch.equal(out_q, out_p)
     # the cached quad follows in-place volume edits
-    sub.layout = "quad"
     sub._image_hu.mul_(2.0)
     out_2 = nd.render(sub, k_inv, rt, sdd, H, W, n_samples=200)
     assert rel_maxabs(out_2, 2 * out_q) < 1e-6
