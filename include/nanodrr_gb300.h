@@ -488,6 +488,21 @@ NDRR_API int32_t ndrr_quad_build_labeled(const void* vol, int32_t vol_dtype, con
 NDRR_API int32_t ndrr_hu_to_mu(const void* hu, int32_t dtype, int64_t n, float mu_water, float mu_bone,
                                float hu_bone, void* mu, void* stream);
 
+/* Camera-space ray endpoints of a detector, one launch: replaces the
+ * reference's _make_tgt / _make_src (src/nanodrr/drr/renderer.py:101-132).
+ * k_inv: n_k (1 or batch) row-major 3x3 inverse intrinsics; sdd: n_s (1 or
+ * batch) source-to-detector distances; all float32 device pointers.
+ * tgt [batch, height*width, 3] = sdd * (K0 * (u + 0.5) + K1 * (v + 0.5) + K2)
+ * for pixel n = v * width + u (Kc: column c of K^-1), each product and sum
+ * rounded on its own, left to right, bitwise the reference's expression in
+ * float32. src: [batch, 1, 3] zeros for a pinhole camera, or [batch,
+ * height*width, 3] = tgt with z - sdd when orthographic != 0. batch must
+ * equal max(n_k, n_s). No counterpart in the reference's C-level
+ * interface. */
+NDRR_API int32_t ndrr_camera_rays(const float* k_inv, int32_t n_k, const float* sdd, int32_t n_s, int32_t batch,
+                                  int32_t height, int32_t width, int32_t orthographic, float* src, float* tgt,
+                                  void* stream);
+
 /* ---- measurement ------------------------------------------------------------ *
  * Kernel timing hook: while set, the calling thread's ray-march entry points
  * record `start` (a cudaEvent_t) on their stream just before each ray-march

@@ -154,6 +154,9 @@ SIGNATURES: dict[str, tuple] = {
     "ndrr_quad_build": (ctypes.c_int32, [ctypes.c_void_p] + [ctypes.c_int32] * 4 + [ctypes.c_void_p] * 2),
     "ndrr_quad_build_labeled": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p]
                                 + [ctypes.c_int32] * 5 + [ctypes.c_void_p] * 2),
+    "ndrr_camera_rays": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+                                          ctypes.c_int32, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]),
     "ndrr_hu_to_mu": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_float, ctypes.c_float,
                                        ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]),
     "ndrr_set_kernel_events": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p]),

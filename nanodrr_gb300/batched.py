@@ -28,7 +28,7 @@ import torch
 from . import _ffi
 from .autotune import BATCHED_CANDIDATES, Autotuner
 from .raymarch import ndrr_dtype
-from .renderer import _affine_product, _make_src, _make_tgt, cached_quad, compact_label
+from .renderer import _affine_product, _camera_rays, cached_quad, compact_label
 
 
 class Request(ctypes.Structure):
@@ -118,8 +118,8 @@ class BatchedRenderer:
         # camera-space rays: pose independent, computed once
         self.src, self.tgt, self.step = [], [], []
         for r in requests:
-            tgt = _make_tgt(r.k_inv, r.sdd, r.height, r.width, self.device, torch.float32).contiguous()
-            src = _make_src(r.orthographic, tgt, r.sdd).contiguous()
+            src, tgt = _camera_rays(r.k_inv, r.sdd, r.height, r.width, r.orthographic, self.device, torch.float32)
+            src, tgt = src.contiguous(), tgt.contiguous()
             step = ((tgt - src).norm(dim=-1) / (r.n_samples - 1)).contiguous()
             self.src.append(src)
             self.tgt.append(tgt)

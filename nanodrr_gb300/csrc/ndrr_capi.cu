@@ -529,6 +529,26 @@ int32_t ndrr_hu_to_mu(const void* hu, int32_t dtype, int64_t n, float mu_water, 
     return ok();
 }
 
+int32_t ndrr_camera_rays(const float* k_inv, int32_t n_k, const float* sdd, int32_t n_s, int32_t batch,
+                         int32_t height, int32_t width, int32_t orthographic, float* src, float* tgt, void* stream) {
+    if (k_inv == nullptr || sdd == nullptr || src == nullptr || tgt == nullptr)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "k_inv, sdd, src and tgt must be non-NULL");
+    if (height < 1 || width < 1 || batch < 1)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "height, width and batch must be >= 1 (got %d, %d, %d)", height, width,
+                    batch);
+    if ((n_k != 1 && n_k != batch) || (n_s != 1 && n_s != batch) || batch != (n_k > n_s ? n_k : n_s))
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "batch %d must be max(n_k, n_s) with each 1 or batch (n_k %d, n_s %d)", batch, n_k,
+                    n_s);
+    if ((long long)batch * height * width * 3 >= (1LL << 31))
+        return fail(NDRR_ERR_LIMIT, "batch x pixels x 3 exceeds int32 indexing");
+    if (misaligned(k_inv, 4) || misaligned(sdd, 4) || misaligned(src, 4) || misaligned(tgt, 4))
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "k_inv, sdd, src and tgt must be 4-byte aligned");
+    const cudaError_t e = ndrr::launch_camera_rays(k_inv, n_k, sdd, n_s, batch, height, width, orthographic != 0, src,
+                                                   tgt, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "camera ray launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
 int32_t ndrr_set_kernel_events(void* start, void* stop) {
     if ((start == nullptr) != (stop == nullptr))
         return fail(NDRR_ERR_INVALID_ARGUMENT, "start and stop events are both set or both NULL");

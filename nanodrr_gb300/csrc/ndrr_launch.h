@@ -62,6 +62,8 @@ cudaError_t launch_homography_bwd(const float* go, const float* img, const float
                                   float* gimg, float* ghom, float* partials, cudaStream_t st);
 cudaError_t launch_batched(const ndrr_batch_args& a, bool backward, int sm_count, cudaStream_t st);
 cudaError_t device_flags(unsigned* out, bool clear);
+cudaError_t launch_camera_rays(const float* k_inv, int n_k, const float* sdd, int n_s, int B, int height, int width,
+                               int orthographic, float* src, float* tgt, cudaStream_t st);
 cudaError_t launch_hu_to_mu(const void* hu, int dtype, long long n, float mu_water, float dmu, float hu_bone,
                             void* mu, cudaStream_t st);
 cudaError_t launch_occupancy(const void* vol, int vol_dtype, int D, int H, int W, int cell, int max_dist,

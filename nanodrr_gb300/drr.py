@@ -26,7 +26,7 @@ import weakref
 import torch
 
 from .geometry import make_k_inv
-from .renderer import _make_src, _make_tgt, render
+from .renderer import _camera_rays, render
 
 
 class DRR(torch.nn.Module):
@@ -52,8 +52,7 @@ class DRR(torch.nn.Module):
             kref, sref, source, built = rec
             if kref() is k and sref() is s and source == self._ray_source():
                 return built
-        tgt = _make_tgt(k, s, int(self.height), int(self.width), k.device, k.dtype)
-        built = (_make_src(bool(self.orthographic), tgt, s), tgt)
+        built = _camera_rays(k, s, int(self.height), int(self.width), bool(self.orthographic), k.device, k.dtype)
         if not (k.requires_grad or s.requires_grad):
             self._ray_record = (weakref.ref(k), weakref.ref(s), self._ray_source(), built)
         return built

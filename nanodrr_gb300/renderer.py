@@ -17,6 +17,7 @@ import weakref
 
 import torch
 
+from . import _ffi
 from .raymarch import (
     fused_raymarch_ex,
     fused_raymarch_ex_forward,
@@ -67,6 +68,44 @@ def _make_src(orthographic: bool, tgt: torch.Tensor, sdd: torch.Tensor) -> torch
         return src
     B = tgt.shape[0]
     return torch.zeros(B, 1, 3, device=tgt.device, dtype=tgt.dtype)
+
+
+def _camera_rays(k_inv, sdd, height, width, orthographic, device, dtype) -> tuple[torch.Tensor, torch.Tensor]:
+    """(src, tgt) of the detector. Float32 CUDA cameras that need no gradient
+    take one `ndrr_camera_rays` launch, which rounds every product and sum as
+    `_make_tgt`/`_make_src` do, so the rays are bitwise the same; other
+    cameras (a differentiable K^-1 or sdd, float64, traced calls) use the
+    tensor expressions."""
+    compiling = hasattr(torch, "compiler") and torch.compiler.is_compiling()
+    if (
+        not compiling
+        and dtype == torch.float32
+        and k_inv.dtype == torch.float32
+        and sdd.dtype == torch.float32
+        and k_inv.device == sdd.device == torch.device(device)
+        and k_inv.is_cuda
+        and k_inv.dim() == 3
+        and tuple(k_inv.shape[1:]) == (3, 3)
+        and sdd.dim() == 1
+        and not (torch.is_grad_enabled() and (k_inv.requires_grad or sdd.requires_grad))
+    ):
+        n_k, n_s = k_inv.shape[0], sdd.shape[0]
+        B = max(n_k, n_s)
+        if n_k in (1, B) and n_s in (1, B):
+            k = k_inv.detach().contiguous()
+            s = sdd.detach().contiguous()
+            N = height * width
+            tgt = torch.empty(B, N, 3, device=k.device, dtype=torch.float32)
+            src = torch.empty(B, N if orthographic else 1, 3, device=k.device, dtype=torch.float32)
+            lib = _ffi.load()
+            _ffi.check(
+                lib.ndrr_camera_rays(k.data_ptr(), n_k, s.data_ptr(), n_s, B, height, width, int(bool(orthographic)),
+                                     src.data_ptr(), tgt.data_ptr(), torch.cuda.current_stream(k.device).cuda_stream),
+                "ndrr_camera_rays",
+            )
+            return src, tgt
+    tgt = _make_tgt(k_inv, sdd, height, width, device, dtype)
+    return _make_src(orthographic, tgt, sdd), tgt
 
 
 def _affine_product(A3: torch.Tensor, rt: torch.Tensor) -> torch.Tensor:
@@ -226,6 +265,8 @@ def render(
         rays = _cached_rays(k_inv, sdd, height, width, n_samples, orthographic, rt_inv)
         if rays is not None:
             return render_cuda(subject, rt_inv, *rays, n_samples, height, width)
+    if tgt is None and src is None:
+        src, tgt = _camera_rays(k_inv, sdd, height, width, orthographic, device, dtype)
     if tgt is None:
         tgt = _make_tgt(k_inv, sdd, height, width, device, dtype)
     if src is None:
@@ -258,8 +299,7 @@ def _cached_rays(k_inv, sdd, height, width, n_samples, orthographic, rt_inv):
                 for t in rays:
                     t.record_stream(stream)
             return rays
-    tgt = _make_tgt(k_inv, sdd, height, width, device, dtype)
-    src = _make_src(orthographic, tgt, sdd)
+    src, tgt = _camera_rays(k_inv, sdd, height, width, orthographic, device, dtype)
     step = (tgt - src).norm(dim=-1) / float(n_samples - 1)
     rays = (src.expand(B, -1, -1).float().contiguous(), tgt.expand(B, -1, -1).float().contiguous(),
             step.expand(B, -1).float().contiguous())

@@ -267,3 +267,14 @@ def test_labelled_quad_validates_on_the_host(lib):
     assert b(0x1000, _ffi.NDRR_BF16, 0x2000, _ffi.NDRR_U8, 3, 4, 4, 4, 0x3008, None) == \
         _ffi.NDRR_ERR_INVALID_ARGUMENT
     assert b(0x1000, _ffi.NDRR_BF16, None, _ffi.NDRR_U8, 3, 4, 4, 4, 0x3000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+
+
+def test_camera_rays_validate_on_the_host(lib):
+    r = lib.ndrr_camera_rays
+    assert r(None, 1, 0x2000, 1, 1, 4, 4, 0, 0x3000, 0x4000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert r(0x1000, 1, 0x2000, 1, 1, 0, 4, 0, 0x3000, 0x4000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert r(0x1000, 2, 0x2000, 3, 3, 4, 4, 0, 0x3000, 0x4000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert r(0x1000, 1, 0x2000, 1, 2, 4, 4, 0, 0x3000, 0x4000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert r(0x1000, 1, 0x2000, 1, 1, 4, 4, 0, 0x3002, 0x4000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert r(0x1000, 1, 0x2000, 1, 40000, 200, 200, 0, 0x3000, 0x4000, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert r(0x1000, 40000, 0x2000, 1, 40000, 200, 200, 0, 0x3000, 0x4000, None) == _ffi.NDRR_ERR_LIMIT

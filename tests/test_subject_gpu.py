@@ -61,3 +61,64 @@ def test_drr_module_equals_render_and_follows_intrinsics():
     assert torch.equal(out2, ref2) and not torch.equal(out2, out)
     drr.width = 32  # a new detector size
     assert drr(sub, rt, n_samples=300).shape == (3, 1, 48, 32)
+
+
+@pytest.mark.parametrize("ortho", [False, True])
+@pytest.mark.parametrize("n_k,n_s", [(1, 1), (3, 1), (1, 3), (3, 3)])
+def test_camera_ray_kernel_is_bitwise_the_tensor_expression(ortho, n_k, n_s):
+    from nanodrr_gb300.renderer import _camera_rays, _make_src, _make_tgt
+
+    g = torch.Generator().manual_seed(n_k * 10 + n_s)
+    k = torch.stack([torch.linalg.inv(torch.tensor([[1000.0 + 50 * i, 0.3, 61.7], [0.0, 990.0 - 7 * i, 45.2],
+                                                   [0.0, 0.0, 1.0]])) for i in range(n_k)])
+    k = (k + 1e-6 * torch.randn(k.shape, generator=g)).to(DEV)
+    s = (1020.0 + 30.0 * torch.rand(n_s, generator=g)).to(DEV)
+    for H, W in [(7, 5), (200, 200), (1, 33)]:
+        src, tgt = _camera_rays(k, s, H, W, ortho, torch.device(DEV), torch.float32)
+        tgt_ref = _make_tgt(k, s, H, W, torch.device(DEV), torch.float32)
+        src_ref = _make_src(ortho, tgt_ref, s)
+        assert tgt.shape == tgt_ref.shape and src.shape == src_ref.shape
+        assert torch.equal(tgt, tgt_ref) and torch.equal(src, src_ref)
+
+
+def test_camera_rays_keep_the_intrinsics_gradient():
+    from nanodrr_gb300.renderer import _camera_rays, _make_tgt
+
+    k = torch.linalg.inv(torch.tensor([[[900.0, 0.0, 50.0], [0.0, 900.0, 40.0], [0.0, 0.0, 1.0]]])).to(DEV)
+    k.requires_grad_(True)
+    s = torch.tensor([1020.0], device=DEV)
+    src, tgt = _camera_rays(k, s, 6, 4, False, torch.device(DEV), torch.float32)
+    assert tgt.requires_grad  # the tensor expressions, not the kernel
+    tgt.sum().backward()
+    assert k.grad is not None and torch.isfinite(k.grad).all()
+    with torch.no_grad():
+        _, t2 = _camera_rays(k, s, 6, 4, False, torch.device(DEV), torch.float32)
+    assert torch.equal(t2, _make_tgt(k.detach(), s, 6, 4, torch.device(DEV), torch.float32))
+
+
+def test_graph_captured_render_follows_intrinsics_edits():
+    ph = phantom.make_phantom((40, 40, 40), (128 / 40,) * 3, seed=3)
+    sub = ph.subject(device=DEV)
+    drr = nd.DRR.from_carm_intrinsics(1020.0, 1.4 * 200 / 48, 1.4 * 200 / 48, 0.0, 0.0, 48, 48, device=DEV)
+    k, s = drr.k_inv.clone(), drr.sdd.clone()
+    rt = phantom.random_poses(1, seed=4).to(DEV)
+    call = lambda: nd.render(sub, k, rt, s, 48, 48, n_samples=300)  # noqa: E731
+    with torch.no_grad():
+        ref = call().clone()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):
+            for _ in range(3):
+                call()
+        torch.cuda.current_stream().wait_stream(side)
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph):
+            out = call()
+        graph.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(out, ref)
+        s.mul_(0.95)  # the graph reads the camera tensors on every replay
+        graph.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(out, call())
+        assert not torch.equal(out, ref)
