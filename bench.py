@@ -210,6 +210,56 @@ def count_samples(M, src, tgt, D, H, W, S):
     return float(n.sum())
 
 
+def warp_cell_sharing(M, src, tgt, D, H, W, S, det, poses=4, warps=512, seed=0):
+    """Lanes per distinct cell among the 32 rays of a warp (8 x 4 detector
+    pixels, the kernels' warp shape) at each iteration of the adjoint's
+    sample loop, where a lane's sample is its ray's first windowed sample
+    plus the iteration (the window rule of count_samples), over a seeded
+    subset of warps: how many of a warp's reductions could merge into one
+    per cell (warp-aggregated atomics)."""
+    dev = M.device
+    g = torch.Generator().manual_seed(seed)
+    n_wx, n_wy = det // 8, det // 4
+    lane = torch.arange(32)
+    lanes = cells = 0
+    for b in range(min(poses, M.shape[0])):
+        wid = torch.randperm(n_wx * n_wy, generator=g)[:warps]
+        px = (wid % n_wx)[:, None] * 8 + lane % 8
+        py = (wid // n_wx)[:, None] * 4 + lane // 8
+        n = (py * det + px).reshape(-1).to(dev)
+        Mb = M[b].double()
+        s_b = src[b].double().expand(tgt.shape[1], -1)[n]
+        d_cam = tgt[b].double()[n] - s_b
+        p0 = s_b @ Mb[:, :3].T + Mb[:, 3]
+        d = d_cam @ Mb[:, :3].T
+        lo_b = torch.tensor([-2.0, -2.0, -2.0], device=dev, dtype=torch.float64)
+        hi_b = torch.tensor([W + 1.0, H + 1.0, D + 1.0], device=dev, dtype=torch.float64)
+        dd = torch.where(d.abs() < 1e-20, torch.full_like(d, 1e-20), d)
+        ta, tb = (lo_b - p0) / dd, (hi_b - p0) / dd
+        t_lo, t_hi = torch.minimum(ta, tb).amax(-1), torch.maximum(ta, tb).amin(-1)
+        f_lo = (torch.floor(t_lo * (S - 1)) - 2).clamp(0, S)
+        f_hi = (torch.ceil(t_hi * (S - 1)) + 3).clamp(0, S)
+        f_hi = torch.where(t_lo <= t_hi, f_hi, f_lo)
+        it = torch.arange(S, device=dev, dtype=torch.float64)
+        s_idx = f_lo[:, None] + it[None, :]  # [rays, iterations]
+        active = s_idx < f_hi[:, None]
+        pos = p0[:, None, :] + (s_idx / (S - 1))[..., None] * d[:, None, :]
+        ix = torch.floor(pos).clamp(min=-2).long()
+        ix = torch.minimum(ix, torch.tensor([W, H, D], device=dev))
+        cid = ((ix[..., 2] + 2) * (H + 3) + (ix[..., 1] + 2)) * (W + 3) + (ix[..., 0] + 2)
+        # inactive lanes get distinct negative ids, then distinct = sorted runs
+        cid = torch.where(active, cid, -1 - torch.arange(cid.numel(), device=dev).reshape(cid.shape))
+        cid = cid.reshape(-1, 32, S).transpose(1, 2)  # [warps, iterations, lanes]
+        act = active.reshape(-1, 32, S).transpose(1, 2)
+        srt = cid.sort(dim=-1).values
+        new = torch.ones_like(srt, dtype=torch.bool)
+        new[..., 1:] = srt[..., 1:] != srt[..., :-1]
+        srt_act = srt >= 0
+        lanes += int(act.sum())
+        cells += int((new & srt_act).sum())
+    return lanes / max(cells, 1)
+
+
 def run_ours(args, world, rank, local):
     import nanodrr_gb300 as nd
     from nanodrr_gb300 import _build
@@ -452,6 +502,18 @@ def run_ours(args, world, rank, local):
         "plain_layout_bwd_ms": round(statistics.median(times["bwd_plain_layout"]), 3),
         "direct_scatter_bwd_ms": round(statistics.median(times["bwd_direct"]), 3),
     }
+    # ---- warp-aggregated reductions: the sharing they can exploit, and the
+    # slab kernel with them (gvol_mode 4) against the default, kernel alone
+    with torch.no_grad():
+        warp_agg = {
+            "lanes_per_cell": round(warp_cell_sharing(M, srcb, tgtb, D, H, W, S, Hd), 3),
+            "how": "32 rays of a warp (8 x 4 pixels) per loop iteration, lane sample = window start + "
+                   "iteration, 512 seeded warps of each of 4 poses",
+            "slab_kernel_ms": round(bwd_kernel_ms, 3),
+            "slab_warp_aggregated_kernel_ms": round(_kernel_only_ms(
+                lambda: raymarch_backward(go, vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd, True, False, gvol=gvol,
+                                          quad=quad, gvol_mode=4), reps), 3),
+        }
     # ---- texture-filtered forward variant (8-bit hardware weights)
     from nanodrr_gb300.raymarch import TextureVolume
 
@@ -543,6 +605,7 @@ def run_ours(args, world, rank, local):
         },
         "samples_per_s": round(n_samp * args.steps * world / t_dev, 1),
         "roofline": roofline,
+        "adjoint_warp_aggregation": warp_agg,
         "e2e": e2e,
         # per step: pose, [proposal network and window check (learned)],
         # forward march, NCC moments, statistics, score and adjoint, slab

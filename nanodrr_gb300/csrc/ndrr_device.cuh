@@ -424,12 +424,16 @@ __device__ __forceinline__ void load_cell_quad_labeled(const void* __restrict__ 
         unpack_quad_f16(make_uint2(q0.x, q0.y), c.v000, c.v001, c.v010, c.v011);
         unpack_quad_f16(make_uint2(q1.x, q1.y), c.v100, c.v101, c.v110, c.v111);
     }
-    const float xc = fminf(fmaxf(x, -2.0f), (float)W + 1.0f);
-    const float yc = fminf(fmaxf(y, -2.0f), (float)H + 1.0f);
-    const float zc = fminf(fmaxf(z, -2.0f), (float)D + 1.0f);
-    const int ox = (int)rintf(xc) - c.ix, oy = (int)rintf(yc) - c.iy, oz = (int)rintf(zc) - c.iz;
-    const unsigned labels = oz ? q1.z : q0.z;
-    c.cls = (int)((labels >> (8 * (ox + 2 * oy))) & 0xffu);
+    // Nearest corner, ties to even: rint of the clamped coordinate minus the
+    // cell's corner, read from the fraction quad_cell already formed (1 past
+    // one half, or at one half on an odd corner). Where the clamp moved the
+    // cell every corner lies outside the volume and carries class 0, so the
+    // choice there cannot change the class.
+    const int ox = (c.fx > 0.5f) | ((c.fx == 0.5f) & (c.ix & 1));
+    const int oy = (c.fy > 0.5f) | ((c.fy == 0.5f) & (c.iy & 1));
+    const int oz = (c.fz > 0.5f) | ((c.fz == 0.5f) & (c.iz & 1));
+    // byte ox + 2 oy of plane oz's class word: one byte permute over both
+    c.cls = (int)(__byte_perm(q0.z, q1.z, (unsigned)(ox + 2 * oy + 4 * oz)) & 0xffu);
 }
 
 // Nearest-voxel label at (x, y, z); ties round to even like grid_sample's
