@@ -765,36 +765,42 @@ def _kernel_only_ms(fn, reps):
     return statistics.median(ts)
 
 
-def l2_read_peak(dev, mib=32, passes=64, reps=7):
+def l2_read_peak(dev, sizes_mib=(16, 32, 48), passes=64, reps=7):
     """Measured L2 read bandwidth (GB/s): the library's probe streams an
-    L2-resident buffer `passes` times with L2-only loads; best of `reps`,
-    CUDA events around each launch."""
+    L2-resident buffer `passes` times with L2-only loads, CUDA events around
+    each launch; the best over `reps` launches of buffers of each size, each
+    allocated afresh (single runs of one 32 MiB buffer have read from 12 to
+    18 TB/s on different boxes)."""
     import ctypes
 
     from nanodrr_gb300 import _ffi
 
     lib = _ffi.load()
-    buf = torch.zeros(mib << 20, dtype=torch.uint8, device=dev)
     sink = torch.zeros(1, dtype=torch.int32, device=dev)
     stream = torch.cuda.current_stream(dev).cuda_stream
-
-    def launch():
-        _ffi.check(lib.ndrr_l2_read_probe(ctypes.c_void_p(buf.data_ptr()), ctypes.c_uint64(buf.numel()), passes,
-                                          ctypes.c_void_p(sink.data_ptr()), ctypes.c_void_p(stream)),
-                   "ndrr_l2_read_probe")
-
-    launch()
-    torch.cuda.synchronize()
     best = 0.0
-    for _ in range(reps):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        launch()
-        e1.record()
+    for mib in sizes_mib:
+        buf = torch.zeros(mib << 20, dtype=torch.uint8, device=dev)
+
+        def launch():
+            _ffi.check(lib.ndrr_l2_read_probe(ctypes.c_void_p(buf.data_ptr()), ctypes.c_uint64(buf.numel()), passes,
+                                              ctypes.c_void_p(sink.data_ptr()), ctypes.c_void_p(stream)),
+                       "ndrr_l2_read_probe")
+
+        for _ in range(3):
+            launch()
         torch.cuda.synchronize()
-        best = max(best, buf.numel() * passes / (e0.elapsed_time(e1) / 1e3) / 1e9)
-    return {"gbs": round(best, 1), "how": f"{mib} MiB buffer read {passes}x with ld.global.cg by 4 CTAs x 512 "
-            f"threads per SM, best of {reps}, CUDA events"}
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            launch()
+            e1.record()
+            torch.cuda.synchronize()
+            best = max(best, buf.numel() * passes / (e0.elapsed_time(e1) / 1e3) / 1e9)
+        del buf
+    sizes = "/".join(str(m) for m in sizes_mib)
+    return {"gbs": round(best, 1), "how": f"{sizes} MiB buffers each read {passes}x with ld.global.cg by 4 CTAs x 512 "
+            f"threads per SM, best of {reps} per size after 3 warm-up launches, CUDA events"}
 
 
 def _rays(sub, rt, k_inv, sdd, det, S):

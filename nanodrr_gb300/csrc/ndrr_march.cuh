@@ -331,17 +331,20 @@ __device__ __forceinline__ void fwd_body(const MarchParams& p, const int tile, c
             run += val;
         }
     };
-    // Two samples per iteration, both cells loaded before either is used, so
-    // two gathers per thread are in flight (label gathers: 3.88 against 4.28
-    // ms at 512 x 512 x 400, 32 poses x 256^2, 8 channels; one channel 2.12
-    // against 2.13). The labelled layout keeps one sample per iteration and
-    // trades registers for occupancy instead (2.88 ms, against 3.31 paired).
+    // Quad layout: two samples per iteration, both cells loaded before either
+    // is used, so two gathers per thread are in flight (label gathers: 3.88
+    // against 4.28 ms at 512 x 512 x 400, 32 poses x 256^2, 8 channels; one
+    // channel 2.12 against 2.13). The labelled layout keeps one sample per
+    // iteration and trades registers for occupancy instead (2.88 ms, against
+    // 3.31 paired), and so does the volume layout, whose one-pose forward is
+    // DRAM-bound and lost resident CTAs to the pair's registers (64 against
+    // 56; 200^2 x 500 samples: 74 against 64 us per graph replay).
     // Positions in float32, p0 + t * d with one rounding: the image is within
     // 1e-6 of the float64 oracle at 512^3 and the loop stays near 56
     // registers (fixed-point positions, which the adjoint uses, measured 28 %
     // slower here: 2.75 against 2.14 ms at 512^3 x 32 x 256^2).
     int s = tr.s0;
-    if constexpr (QUAD != kLayoutQuadLab) {
+    if constexpr (QUAD == kLayoutQuad) {
         for (; s + 1 < tr.s1; s += 2) {
             const float ta = (float)s * p.inv_s, tb = (float)(s + 1) * p.inv_s;
             const float xa = fmaf(ta, tr.ray.dx, tr.ray.p0x), xb = fmaf(tb, tr.ray.dx, tr.ray.p0x);
@@ -415,11 +418,24 @@ __device__ __forceinline__ void fwd_body(const MarchParams& p, const int tile, c
     }
 }
 
+// Register budget of the forward per instantiation, set for occupancy: the
+// loop is latency-bound, and more resident warps pay until spills cost more
+// (kernel alone, 512 x 512 x 400 f32 / bf16, 32 poses x 256^2, 800 samples):
+// f32 quad, one channel: 2.02 ms at 48 registers (10 CTAs of 128 per SM)
+// against 2.10 at 56 and 2.41 at 40; f32 quad, 8 channels with label
+// gathers: 3.77 at 40 against 3.81 at 48 and 3.93 at 64; labelled quad
+// (bf16, 8 channels): 2.88 at 40 against 2.99 at 48 and 3.18 at 52; the
+// volume layout: 3.59 at 64 against 3.83 at 48. Others keep 64 (two CTAs of
+// 512 threads per SM).
+template <typename VT, bool MULTI, int QUAD>
+struct FwdRegs {
+    static constexpr int value = QUAD == kLayoutQuadLab ? 40
+                                 : (QUAD == kLayoutQuad && std::is_same<VT, float>::value) ? (MULTI ? 40 : 48)
+                                                                                            : 64;
+};
+
 template <typename VT, typename OT, bool MULTI, int SKIP, int QUAD>
-// The labelled layout's forward runs at three CTAs of 512 threads per SM (at
-// most 42 registers): 2.88 against 3.18 ms at two (8 channels, 512 x 512 x
-// 400, 32 poses x 256^2); the other layouts lose occupancy's gain to spills.
-__global__ void __launch_bounds__(512, QUAD == kLayoutQuadLab ? 3 : 2) raymarch_fwd_kernel(const MarchParams p) {
+__global__ void __maxnreg__((FwdRegs<VT, MULTI, QUAD>::value)) raymarch_fwd_kernel(const MarchParams p) {
     fwd_body<VT, OT, MULTI, SKIP, QUAD>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles);
 }
 
