@@ -874,8 +874,20 @@ __device__ __forceinline__ void bwd_body(const MarchParams& p, const int tile, c
     adjoint_epilogue<GCAM>(p, slot, tr, A, smem, R, NT, r, k);
 }
 
+// Register budget of the adjoint: 128 (one CTA of 512 threads per SM), but
+// 56 for the one-channel pose-only adjoint of an f32 quad volume without an
+// in-kernel skip, where occupancy pays: 2.80 against 2.86 ms at 70
+// registers (512^3, 32 poses x 256^2, 800 samples, kernel alone; 64
+// measured 3.16).
 template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP, int QUAD>
-__global__ void __launch_bounds__(512, 1) raymarch_bwd_kernel(const MarchParams p) {
+struct BwdRegs {
+    static constexpr int value =
+        (!MULTI && !GVOL && !GCAM && SKIP == 0 && QUAD == kLayoutQuad && std::is_same<VT, float>::value) ? 56
+                                                                                                          : 128;
+};
+
+template <typename VT, bool MULTI, bool GVOL, bool GCAM, int SKIP, int QUAD>
+__global__ void __maxnreg__((BwdRegs<VT, MULTI, GVOL, GCAM, SKIP, QUAD>::value)) raymarch_bwd_kernel(const MarchParams p) {
     bwd_body<VT, MULTI, GVOL, GCAM, SKIP, QUAD>(p, blockIdx.x % p.tm.tiles, blockIdx.x / p.tm.tiles, blockIdx.x);
 }
 
