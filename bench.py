@@ -765,12 +765,13 @@ def _kernel_only_ms(fn, reps):
     return statistics.median(ts)
 
 
-def l2_read_peak(dev, sizes_mib=(16, 32, 48), passes=64, reps=7):
+def l2_read_peak(dev, sizes_mib=(16, 32, 48), passes=256, reps=10, warm_ms=100.0):
     """Measured L2 read bandwidth (GB/s): the library's probe streams an
     L2-resident buffer `passes` times with L2-only loads, CUDA events around
     each launch; the best over `reps` launches of buffers of each size, each
-    allocated afresh (single runs of one 32 MiB buffer have read from 12 to
-    18 TB/s on different boxes)."""
+    allocated afresh, after about `warm_ms` of back-to-back launches so the
+    clocks have left any idle state (a 2 ms probe read 12 to 20 TB/s on
+    different runs)."""
     import ctypes
 
     from nanodrr_gb300 import _ffi
@@ -787,7 +788,13 @@ def l2_read_peak(dev, sizes_mib=(16, 32, 48), passes=64, reps=7):
                                               ctypes.c_void_p(sink.data_ptr()), ctypes.c_void_p(stream)),
                        "ndrr_l2_read_probe")
 
-        for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        launch()
+        e1.record()
+        torch.cuda.synchronize()
+        n_warm = max(3, min(2000, int(warm_ms / max(e0.elapsed_time(e1), 1e-3))))
+        for _ in range(n_warm):
             launch()
         torch.cuda.synchronize()
         for _ in range(reps):
@@ -800,7 +807,7 @@ def l2_read_peak(dev, sizes_mib=(16, 32, 48), passes=64, reps=7):
         del buf
     sizes = "/".join(str(m) for m in sizes_mib)
     return {"gbs": round(best, 1), "how": f"{sizes} MiB buffers each read {passes}x with ld.global.cg by 4 CTAs x 512 "
-            f"threads per SM, best of {reps} per size after 3 warm-up launches, CUDA events"}
+            f"threads per SM, best of {reps} per size after ~{warm_ms:.0f} ms of warm-up launches, CUDA events"}
 
 
 def _rays(sub, rt, k_inv, sdd, det, S):
