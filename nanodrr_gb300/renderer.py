@@ -77,13 +77,16 @@ def _camera_rays(k_inv, sdd, height, width, orthographic, device, dtype) -> tupl
     cameras (a differentiable K^-1 or sdd, float64, traced calls) use the
     tensor expressions."""
     compiling = hasattr(torch, "compiler") and torch.compiler.is_compiling()
+    want = torch.device(device)
     if (
         not compiling
         and dtype == torch.float32
         and k_inv.dtype == torch.float32
         and sdd.dtype == torch.float32
-        and k_inv.device == sdd.device == torch.device(device)
         and k_inv.is_cuda
+        and k_inv.device == sdd.device
+        and want.type == "cuda"
+        and (want.index is None or want == k_inv.device)
         and k_inv.dim() == 3
         and tuple(k_inv.shape[1:]) == (3, 3)
         and sdd.dim() == 1
