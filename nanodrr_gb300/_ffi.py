@@ -29,7 +29,7 @@ NDRR_F32, NDRR_F16, NDRR_BF16, NDRR_U8, NDRR_I8, NDRR_I16, NDRR_I32, NDRR_I64 = 
 ABI_VERSION = 3
 
 # ndrr_gvol_mode
-NDRR_GVOL_AUTO, NDRR_GVOL_DIRECT, NDRR_GVOL_BRICK, NDRR_GVOL_SLAB, NDRR_GVOL_SLAB_WARP = 0, 1, 2, 3, 4
+NDRR_GVOL_AUTO, NDRR_GVOL_DIRECT, NDRR_GVOL_BRICK, NDRR_GVOL_SLAB, NDRR_GVOL_SLAB_WARP, NDRR_GVOL_SPLIT = 0, 1, 2, 3, 4, 5
 
 _c_float_p = ctypes.POINTER(ctypes.c_float)
 

@@ -69,6 +69,29 @@ cudaError_t launch_bwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaS
             e = cudaMemsetAsync(a.gvol_quad, 0, (size_t)(a.D + 4) * (a.H + 3) * (a.W + 3) * 16, st);
             if (e != cudaSuccess) return e;
         }
+        if (gvol && ls.split) {
+            // split adjoint: the pose pass (gathers; the call's skip or
+            // sample windows drop only samples without pose terms), then
+            // the positions-only scatter pass in slab order, then the fold.
+            // The kernel events, when set, bracket both march passes.
+            KernelEvents& ev = kernel_events();
+            const KernelEvents outer = ev;
+            ev = KernelEvents{};
+            MarchParams pp = p;
+            pp.partials = slab_partials(a, ls);
+            if (outer.start != nullptr) cudaEventRecord(outer.start, st);
+            e = launch_bwd_quad(pp, a.vol_dtype, false, false, false, a.skip_mode, a.quad_labels != 0, grid, block,
+                                bwd_smem_bytes(a, ls), st);
+            if (e == cudaSuccess) {
+                pose_partials_reduce_kernel<<<a.B, 256, 0, st>>>(pp.partials, p.tm.tiles, a.gM, nullptr);
+                e = cudaGetLastError();
+            }
+            if (e == cudaSuccess) e = launch_scatter_slab(a, ls, p, st);
+            if (e == cudaSuccess && outer.stop != nullptr) e = cudaEventRecord(outer.stop, st);
+            ev = outer;
+            if (e == cudaSuccess) e = launch_quad_fold(a.gvol_quad, a.D, a.H, a.W, a.gvol, a.gvol_overwrite != 0, st);
+            return e;
+        }
         if (gvol && ls.slab) {
             // slab-ordered adjoint: writes gM itself (ndrr_slab.cu)
             e = launch_bwd_slab(a, ls, p, st);

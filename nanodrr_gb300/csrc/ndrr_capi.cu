@@ -161,9 +161,10 @@ int32_t validate_common(const ndrr_raymarch_args* a) {
         return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_overwrite is 0, or 1 with the quad layout");
     if (a->fwd_mode != NDRR_FWD_DEFAULT && a->fwd_mode != NDRR_FWD_TMA)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "fwd_mode must be 0 or 1 (got %d)", a->fwd_mode);
-    if (a->gvol_mode < NDRR_GVOL_AUTO || a->gvol_mode > NDRR_GVOL_SLAB_WARP)
-        return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode must be 0 .. 4 (got %d)", a->gvol_mode);
-    if ((a->gvol_mode == NDRR_GVOL_SLAB || a->gvol_mode == NDRR_GVOL_SLAB_WARP) && a->vol_quad == nullptr)
+    if (a->gvol_mode < NDRR_GVOL_AUTO || a->gvol_mode > NDRR_GVOL_SPLIT)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode must be 0 .. 5 (got %d)", a->gvol_mode);
+    if ((a->gvol_mode == NDRR_GVOL_SLAB || a->gvol_mode == NDRR_GVOL_SLAB_WARP || a->gvol_mode == NDRR_GVOL_SPLIT) &&
+        a->vol_quad == nullptr)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "gvol_mode 3 and 4 (slab-ordered) need the quad layout (vol_quad)");
     if (a->brick_cap < 0 || a->brick_cap > 56 * 1024)
         return fail(NDRR_ERR_INVALID_ARGUMENT, "brick capacity %d out of range [0, 57344] voxels", a->brick_cap);
@@ -278,16 +279,20 @@ int32_t ndrr_raymarch_bwd_workspace_bytes(const ndrr_raymarch_args* a, uint64_t*
 
 int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* a, void* stream) {
     int32_t rc = validate_common(a);
-    if (rc == NDRR_OK && !a->need_gvol) rc = reject_proposal_march(a);
+    if (rc != NDRR_OK) return rc;
+    // the split adjoint's pose pass honours the skip like a pose-only adjoint
+    const bool split = a->need_gvol && ndrr::choose_shape(*a, 0).split;
+    if (!a->need_gvol || split) rc = reject_proposal_march(a);
     if (rc != NDRR_OK) return rc;
     if (a->B == 0 || a->N == 0) return ok();
     if (a->go == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "go is NULL");
     if (!is_float_dtype(a->go_dtype)) return fail(NDRR_ERR_DTYPE, "go dtype %d unsupported", a->go_dtype);
     if (a->gM == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "gM is NULL");
     if (a->need_gvol && a->gvol == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "need_gvol set but gvol is NULL");
-    if (a->need_gvol && a->sample_window != nullptr)
+    if (a->need_gvol && a->sample_window != nullptr && !split)
         return fail(NDRR_ERR_INVALID_ARGUMENT,
-                    "sample_window cannot be combined with need_gvol: the volume gradient needs every sample");
+                    "sample_window with need_gvol needs gvol_mode 5 (split passes): the volume gradient needs every "
+                    "sample, and only the split adjoint's pose pass can use windows");
     if (a->need_gcam && (a->gsrc == nullptr || a->gtgt == nullptr || a->gstep == nullptr))
         return fail(NDRR_ERR_INVALID_ARGUMENT, "need_gcam set but gsrc/gtgt/gstep is NULL");
     if (a->vol_quad != nullptr && a->need_gvol && a->gvol_quad == nullptr)

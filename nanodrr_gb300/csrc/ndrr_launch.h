@@ -17,6 +17,7 @@ struct LaunchShape {
     int L0 = 16;         // initial slab length in samples
     int sm = 0;          // SM count of the device (0 when unknown)
     bool slab = false;   // adjoint with volume gradient ordered slab by slab (quad layout)
+    bool split = false;  // slab: pose pass with gathers, then a positions-only scatter pass
 };
 
 // Measurement hook (ndrr_set_kernel_events): CUDA events recorded on the
@@ -45,6 +46,7 @@ cudaError_t texture_create(const float* vol, int D, int H, int W, unsigned long 
 cudaError_t texture_destroy(unsigned long long handle, bool* known);
 cudaError_t launch_bwd(const ndrr_raymarch_args& a, const LaunchShape& ls, cudaStream_t st);
 uint64_t slab_workspace_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
+float* slab_partials(const ndrr_raymarch_args& a, const LaunchShape& ls);
 int homography_blocks(int H, int W);
 size_t ncc_workspace_bytes(int B, int P, int N);
 cudaError_t launch_ncc_fwd(const float* x1, const float* x2, int B, int P, int N, float eps, float* score,

@@ -1040,6 +1040,8 @@ cudaError_t launch_quad_build_labeled(const void* vol, int dtype, const void* la
 MarchParams make_params(const ndrr_raymarch_args& a, const LaunchShape& ls);
 cudaError_t launch_bwd_slab(const ndrr_raymarch_args& a, const LaunchShape& ls, const MarchParams& p,
                             cudaStream_t st);
+cudaError_t launch_scatter_slab(const ndrr_raymarch_args& a, const LaunchShape& ls, const MarchParams& p0,
+                                cudaStream_t st);
 size_t fwd_base_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);
 
 template <typename Kern>

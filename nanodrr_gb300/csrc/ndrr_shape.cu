@@ -94,7 +94,9 @@ LaunchShape choose_shape(const ndrr_raymarch_args& a, int sm_count) {
     // without camera gradients; measured 11 % faster than direct scatter at
     // 512^3 x 32 poses).
     ls.slab = (a.gvol_mode == NDRR_GVOL_SLAB || a.gvol_mode == NDRR_GVOL_SLAB_WARP ||
-               a.gvol_mode == NDRR_GVOL_AUTO) && a.vol_quad != nullptr && a.need_gvol && !a.need_gcam;
+               a.gvol_mode == NDRR_GVOL_SPLIT || a.gvol_mode == NDRR_GVOL_AUTO) &&
+              a.vol_quad != nullptr && a.need_gvol && !a.need_gcam;
+    ls.split = ls.slab && a.gvol_mode == NDRR_GVOL_SPLIT && a.n_classes == 1;
     if (ls.brick) {
         ls.K = 1;
         const int nt = ls.tw * ls.th;

@@ -235,6 +235,51 @@ __global__ void __launch_bounds__(512, 1) raymarch_bwd_slab_kernel(const MarchPa
     }
 }
 
+// Volume-gradient scatter of one (slab, pose, tile) item from sample
+// positions alone: the split adjoint's second pass. The terms are those of
+// adjoint_accumulate's scatter (go * step * trilinear weight per corner, two
+// 16-byte reductions into the quad gradient per sample); the volume values
+// and the pose terms, which need the gathers, come from the first pass.
+__device__ __forceinline__ void scatter_body(const MarchParams& p, const int tile, const int b,
+                                             const SlabCut cut) {
+    const int n = tile_ray(p.tm, p.N, p.tw, p.th, tile, (int)threadIdx.x);
+    if (n < 0) return;
+    float m[12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) m[j] = __ldg(p.M + (size_t)b * 12 + j);
+    ThreadRay tr;
+    init_thread_ray(p, m, b, n, tr);
+    restrict_to_slab(p, tr, cut);
+    const float go = ld_any_f(p.go, p.go_dtype, tr.bn);
+    if (go == 0.f) return;  // every term is proportional to go
+    const float g = go * tr.stepv;
+    const QuadScatter sc{p.gquad, p.qg};
+    for (int s = tr.ray.lo; s < tr.ray.hi; ++s) {
+        Cell c;
+        fix_cell(fix_at(tr, s), p.D, p.H, p.W, c);
+        const float wy0 = 1.f - c.fy, wz0 = 1.f - c.fz;
+        sc(0, c.ix, c.iy, c.iz, g * wz0 * wy0, g * wz0 * c.fy, g * c.fz * wy0, g * c.fz * c.fy, 1.f - c.fx, c.fx);
+    }
+}
+
+__global__ void __launch_bounds__(512) raymarch_scatter_slab_kernel(const MarchParams p, const SlabParams s) {
+    __shared__ int item_sh;
+    const int total = s.counters[0];
+    while (true) {
+        __syncthreads();  // every thread has read item_sh
+        if (threadIdx.x == 0) item_sh = atomicAdd(&s.counters[1], 1);
+        __syncthreads();
+        const int item = item_sh;
+        if (item >= total) break;
+        const int2 it = s.items[item];
+        const int bt = it.x, k = it.y;
+        const int b = bt / p.tm.tiles, tile = bt % p.tm.tiles;
+        const int axis = s.axis[b];
+        const int thick = axis == 0 ? s.Z[0] : (axis == 1 ? s.Z[1] : s.Z[2]);
+        scatter_body(p, tile, b, SlabCut{axis, k * thick, (k + 1) * thick});
+    }
+}
+
 // Per-pose fixed-order sum of the item partials: thread j of the CTA takes
 // tiles j, j + 256, ... in order and each tile's slabs in order.
 __global__ void __launch_bounds__(256) slab_pose_reduce_kernel(const SlabParams s, int tiles, float* __restrict__ gM) {
@@ -289,14 +334,12 @@ static cudaError_t launch_slab_march(const MarchParams& p, const SlabParams& s, 
     return e;
 }
 
-// Slab-ordered adjoint with volume gradient for the quad layout; writes gM
-// and scatters into p.gquad (zeroed by the caller, folded afterwards).
-cudaError_t launch_bwd_slab(const ndrr_raymarch_args& a, const LaunchShape& ls, const MarchParams& p0,
-                            cudaStream_t st) {
-    MarchParams p = p0;
+// Work list of a slab-ordered pass: the slab geometry and workspace carving
+// in `s`, then the plan, scan and fill kernels on `st`.
+static cudaError_t slab_setup(const ndrr_raymarch_args& a, const LaunchShape& ls, const MarchParams& p,
+                              SlabParams& s, cudaStream_t st) {
     const SlabLayout L = slab_layout(a, ls);
     unsigned char* ws = reinterpret_cast<unsigned char*>(a.workspace);
-    SlabParams s;
     slab_geometry(a, s.Z, s.ns);
     s.base[0] = 0;
     s.base[1] = s.ns[0];
@@ -311,9 +354,6 @@ cudaError_t launch_bwd_slab(const ndrr_raymarch_args& a, const LaunchShape& ls, 
     s.axis = reinterpret_cast<int*>(ws + L.axis);
     s.items = reinterpret_cast<int2*>(ws + L.items);
     s.partials = reinterpret_cast<float*>(ws + L.partials);
-    p.partials = s.partials;
-    p.K = 1;  // items are short: one thread per ray
-
     cudaError_t e = cudaMemsetAsync(s.hist, 0, (size_t)s.ns_total * sizeof(int), st);
     if (e != cudaSuccess) return e;
     const int R = p.tw * p.th;
@@ -322,7 +362,47 @@ cudaError_t launch_bwd_slab(const ndrr_raymarch_args& a, const LaunchShape& ls, 
     slab_scan_kernel<<<1, 1024, 0, st>>>(s);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     slab_fill_kernel<<<(s.BT + 255) / 256, 256, 0, st>>>(s, p.tm.tiles);
-    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+// The slab layout's partials region, which the split adjoint's pose pass
+// uses for its per-tile partials (it holds at least one slot per tile).
+float* slab_partials(const ndrr_raymarch_args& a, const LaunchShape& ls) {
+    return reinterpret_cast<float*>(reinterpret_cast<unsigned char*>(a.workspace) + slab_layout(a, ls).partials);
+}
+
+// The split adjoint's scatter pass: slab-ordered, every sample of the cull
+// window (no skip, no sample windows), into p.gquad (zeroed by the caller).
+cudaError_t launch_scatter_slab(const ndrr_raymarch_args& a, const LaunchShape& ls, const MarchParams& p0,
+                                cudaStream_t st) {
+    MarchParams p = p0;
+    p.win = nullptr;
+    p.K = 1;
+    SlabParams s;
+    cudaError_t e = slab_setup(a, ls, p, s, st);
+    if (e != cudaSuccess) return e;
+    const int block = p.tw * p.th;
+    int dev = 0, sms = 0, per_sm = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, raymarch_scatter_slab_kernel, block, 0);
+    if (e != cudaSuccess) return e;
+    const unsigned grid = (unsigned)std::max(1, sms * std::max(per_sm, 1));
+    raymarch_scatter_slab_kernel<<<grid, block, 0, st>>>(p, s);
+    return cudaGetLastError();
+}
+
+// Slab-ordered adjoint with volume gradient for the quad layout; writes gM
+// and scatters into p.gquad (zeroed by the caller, folded afterwards).
+cudaError_t launch_bwd_slab(const ndrr_raymarch_args& a, const LaunchShape& ls, const MarchParams& p0,
+                            cudaStream_t st) {
+    MarchParams p = p0;
+    p.K = 1;  // items are short: one thread per ray
+    SlabParams s;
+    cudaError_t e = slab_setup(a, ls, p, s, st);
+    if (e != cudaSuccess) return e;
+    p.partials = s.partials;
+    const int R = p.tw * p.th;
     const size_t smem = bwd_epilogue_bytes(a, ls);
     const bool multi = a.n_classes > 1;
     const bool agg = a.gvol_mode == NDRR_GVOL_SLAB_WARP;

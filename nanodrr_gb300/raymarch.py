@@ -407,15 +407,18 @@ def raymarch_backward(
     accumulated into (so several calls can share one); otherwise a zeroed one
     is allocated. `gvol_mode` selects the volume-gradient scatter (0 auto,
     1 direct atomics, 2 per-slab shared-memory brick, 3 slab-ordered work,
-    which auto picks for the quad layout without camera gradients),
+    which auto picks for the quad layout without camera gradients, 4 slab
+    with warp aggregation, 5 split: a pose pass that gathers, then a
+    slab-ordered scatter pass from sample positions alone),
     `slab_mib` the quad-gradient MiB per slab (0 = default), `brick_cap` the brick
     capacity in voxels (0 = default) and `tile` an explicit
     (tile_w, tile_h, sample_split) launch shape. Skips and `windows` apply to
-    the pose/camera adjoint only: with `need_gvol` every sample is marched."""
+    the pose/camera adjoint only: with `need_gvol` every sample is marched
+    (gvol_mode 5 applies them to its pose pass)."""
     _check_inputs(vol, lab, M, src, tgt, step, n_samples, n_classes)
     vol, lab, M, src, tgt, step = _prep(vol, lab, M, src, tgt, step)
     B, N, _ = tgt.shape
-    if need_gvol:
+    if need_gvol and gvol_mode != _ffi.NDRR_GVOL_SPLIT:
         skip, windows = None, None
     elif _windows_route(skip):
         if windows is None:

@@ -235,3 +235,35 @@ def test_render_rebuilds_a_stale_grid():
         ref = nd.render(sub, k_inv, rt, sdd, det, det, n_samples=n)
     assert not torch.equal(a, ref)
     assert rel_maxabs(b, ref) < 1e-6
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_split_adjoint_pose_pass_uses_the_skip(fused):
+    """gvol_mode 5: the pose pass (the gathers) honours the occupancy skip —
+    as an in-kernel window or as sample windows — whose skipped samples carry
+    no pose terms, while the positions-only scatter pass marches every
+    sample: gM as without the skip (bitwise with sample windows and one thread
+    per ray), the volume
+    gradient equal to the slab-ordered adjoint's to rounding."""
+    from nanodrr_gb300.raymarch import quad_volume
+
+    ph, sub, vol, lab, M, src, tgt, step, n, det, *_ = _case(B=5)
+    q = quad_volume(vol)
+    go = torch.randn(5, 1, det * det, device=DEV, generator=torch.Generator(device=DEV).manual_seed(3))
+    args = (go, vol, vol, M, src, tgt, step, n, 1, det, True, False)
+    slab = raymarch_backward(*args, quad=q, gvol_mode=3)
+    split = raymarch_backward(*args, quad=q, gvol_mode=5)
+    again = raymarch_backward(*args, quad=q, gvol_mode=5)
+    assert rel_maxabs(split[0], slab[0]) < 1e-5
+    assert rel_maxabs(split[1], slab[1]) < 1e-5
+    assert torch.equal(split[1], again[1])
+    skip = EmptySpace.occupancy(vol, cell=4, fused=fused)
+    sk = raymarch_backward(*args, quad=q, gvol_mode=5, skip=skip)
+    # this small launch splits each ray's samples over several threads, whose
+    # chunks follow the window: the pose gradient regroups
+    assert rel_maxabs(sk[1], split[1]) < 1e-5
+    assert rel_maxabs(sk[0], slab[0]) < 1e-5
+    if not fused:  # one thread per ray: sample windows drop only zero terms
+        one = raymarch_backward(*args, quad=q, gvol_mode=5, tile=(16, 8, 1))
+        one_sk = raymarch_backward(*args, quad=q, gvol_mode=5, tile=(16, 8, 1), skip=skip)
+        assert torch.equal(one_sk[1], one[1])
