@@ -196,7 +196,7 @@ typedef struct ndrr_raymarch_args {
     int32_t brick_cap;      /* gvol_mode 2: brick capacity in voxels (0 default,
                                at most 57344)                                   */
     int32_t slab_mib;       /* gvol_mode 3 (and auto): quad-gradient MiB per
-                               slab (0 default = 96, at most 4096)              */
+                               slab (0 default = 128, at most 4096)              */
     int32_t fwd_mode;       /* NDRR_FWD_* (0 default)                          */
     int32_t gvol_overwrite; /* quad layout only: 1 = the adjoint writes gvol
                                instead of accumulating into it (no zeroing
@@ -242,7 +242,7 @@ enum ndrr_skip_mode {
     NDRR_SKIP_PROPOSAL = 2,
 };
 
-/* NDRR_GVOL_SLAB: the volume is cut into slabs (about 96 MB of quad
+/* NDRR_GVOL_SLAB: the volume is cut into slabs (about 128 MB of quad
  * gradient each) along one axis per pose, and (slab, pose, tile) work items
  * run slab by slab across all poses, so that a slab's lines are reused from
  * L2 by every pose before eviction. It is what NDRR_GVOL_AUTO selects for
