@@ -45,7 +45,7 @@ METRIC = "fwd+bwd DRR frames/s at 512^3/256^2, learned-skip vs plain kernel"
 # measured by ncu (dram__bytes_read.sum + dram__bytes_write.sum of one launch)
 # on a 384^3 x 8-pose case of the same kernel and scaled here by the samples
 # of a launch.
-SLAB_DRAM_BYTES_PER_SAMPLE = 25.57
+SLAB_DRAM_BYTES_PER_SAMPLE = 19.67
 SLAB_DRAM_SOURCE = "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch, 384^3 x 8 poses, scaled per sample"
 
 
