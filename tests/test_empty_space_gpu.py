@@ -237,8 +237,9 @@ def test_render_rebuilds_a_stale_grid():
     assert rel_maxabs(b, ref) < 1e-6
 
 
+@pytest.mark.parametrize("dtype", [torch.float32, torch.bfloat16])
 @pytest.mark.parametrize("fused", [True, False])
-def test_split_adjoint_pose_pass_uses_the_skip(fused):
+def test_split_adjoint_pose_pass_uses_the_skip(fused, dtype):
     """gvol_mode 5: the pose pass (the gathers) honours the occupancy skip —
     as an in-kernel window or as sample windows — whose skipped samples carry
     no pose terms, while the positions-only scatter pass marches every
@@ -248,6 +249,7 @@ def test_split_adjoint_pose_pass_uses_the_skip(fused):
     from nanodrr_gb300.raymarch import quad_volume
 
     ph, sub, vol, lab, M, src, tgt, step, n, det, *_ = _case(B=5)
+    vol = vol.to(dtype)
     q = quad_volume(vol)
     go = torch.randn(5, 1, det * det, device=DEV, generator=torch.Generator(device=DEV).manual_seed(3))
     args = (go, vol, vol, M, src, tgt, step, n, 1, det, True, False)
