@@ -36,6 +36,13 @@ _BACKENDS = ("auto", "cuda", "triton")
 _RAY_CACHE: dict = {}
 _RAY_CACHE_SIZE = 4
 
+# Camera -> voxel affines of recent calls without a gradient, keyed by the
+# world_to_voxel and rt_inv tensor objects: a repeated render of the same
+# pose reuses M instead of two tensor launches (~25 us of host time per call).
+# Valid while both tensors are alive and unmodified, as for the ray cache.
+_M_CACHE: dict = {}
+_M_CACHE_SIZE = 4
+
 
 def fused_supported(subject: Subject, B: int, n_pixels: int) -> bool:
     """Limits of the CUDA kernels: one volume, int32 voxel and ray indexing
@@ -117,6 +124,31 @@ def _affine_product(A3: torch.Tensor, rt: torch.Tensor) -> torch.Tensor:
     return (A3[None, :, :, None] * rt[:, None, :, :]).sum(dim=2)
 
 
+def _call_affine(w2v: torch.Tensor, rt_inv: torch.Tensor, grad: bool) -> torch.Tensor:
+    """M = (world_to_voxel @ rt_inv)[:, :3] in float32 (`_affine_product`),
+    from the affine cache when no gradient is recorded and nothing is traced
+    or captured into a CUDA graph (a graph must read rt_inv on every replay)."""
+    if (grad or (hasattr(torch, "compiler") and torch.compiler.is_compiling())
+            or rt_inv.device.type != "cuda" or torch.cuda.is_current_stream_capturing()):
+        return _affine_product(w2v.float()[:3], rt_inv.float())
+    stream = torch.cuda.current_stream(rt_inv.device)
+    key = (id(w2v), id(rt_inv))
+    hit = _M_CACHE.get(key)
+    if hit is not None:
+        wref, wver, rref, rver, M, made_on = hit
+        if wref() is w2v and rref() is rt_inv and wver == w2v._version and rver == rt_inv._version:
+            if stream != made_on:  # keep the allocator from reusing it under this stream's kernels
+                M.record_stream(stream)
+            return M
+    M = _affine_product(w2v.float()[:3], rt_inv.float())
+    for k in [k for k, v in _M_CACHE.items() if v[0]() is None or v[2]() is None]:
+        del _M_CACHE[k]  # entries whose tensors are gone
+    while len(_M_CACHE) >= _M_CACHE_SIZE:
+        _M_CACHE.pop(next(iter(_M_CACHE)))
+    _M_CACHE[key] = (weakref.ref(w2v), w2v._version, weakref.ref(rt_inv), rt_inv._version, M, stream)
+    return M
+
+
 def compact_label(subject: Subject) -> torch.Tensor:
     """Label map for the kernels: float labels with n_classes <= 255 are packed
     to uint8 once per label tensor version (trunc(label) if it is a class in
@@ -146,13 +178,13 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
     # index ([0, 0]) would allocate and zero a volume-sized gradient per level.
     vol = (img.reshape(img.shape[-3:]) if img.shape[:2] == (1, 1) else img[0, 0]).contiguous()
     lab = compact_label(subject) if C > 1 else vol
-    M = _affine_product(subject.world_to_voxel.float()[:3], rt_inv.float())
     # With a gradient recorded, the adjoint forms sample positions from M +
     # M_lo in float-float and carries them in fixed point
     # (ndrr_raymarch_args.M_lo): M_lo is the float32 product's error against
     # the float64 affine of the same inputs. The forward reads float32 M only,
     # so a call without a gradient skips the float64 product.
     grad = torch.is_grad_enabled() and any(t.requires_grad for t in (vol, rt_inv, src, tgt, step_size))
+    M = _call_affine(subject.world_to_voxel, rt_inv, grad)
     if grad:
         M64 = _affine_product(subject.world_to_voxel.detach().double()[:3], rt_inv.detach().double())
         M_lo = (M64 - M.detach().double()).float()

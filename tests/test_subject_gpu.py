@@ -122,3 +122,26 @@ def test_graph_captured_render_follows_intrinsics_edits():
         torch.cuda.synchronize()
         assert torch.equal(out, call())
         assert not torch.equal(out, ref)
+
+
+def test_affine_cache_follows_pose_edits():
+    """A repeated render without a gradient reuses the camera -> voxel affine
+    of the same pose tensor; an in-place pose edit or a new tensor rebuilds
+    it, and a render with a gradient never reads the cache."""
+    ph = phantom.make_phantom((40, 40, 40), (128 / 40,) * 3, seed=5)
+    sub = ph.subject(device=DEV)
+    drr = nd.DRR.from_carm_intrinsics(1020.0, 1.4 * 200 / 32, 1.4 * 200 / 32, 0.0, 0.0, 32, 32, device=DEV)
+    k, s = drr.k_inv, drr.sdd
+    rt = phantom.random_poses(2, seed=6).to(DEV)
+    with torch.no_grad():
+        a = nd.render(sub, k, rt, s, 32, 32, n_samples=200)
+        assert torch.equal(nd.render(sub, k, rt, s, 32, 32, n_samples=200), a)
+        rt[:, :3, 3] += 5.0  # in place: the cached affine is stale
+        c = nd.render(sub, k, rt, s, 32, 32, n_samples=200)
+        assert torch.equal(c, nd.render(sub, k, rt.clone(), s, 32, 32, n_samples=200))
+        assert not torch.equal(c, a)
+    rtg = rt.clone().requires_grad_(True)
+    g = nd.render(sub, k, rtg, s, 32, 32, n_samples=200)
+    assert torch.equal(g.detach(), c)
+    g.sum().backward()
+    assert rtg.grad is not None and torch.isfinite(rtg.grad).all()
