@@ -424,6 +424,7 @@ def run_ours(args, world, rank, local):
         fwd_kernel_ms = _kernel_only_ms(lambda: raymarch_forward(vol, vol, M, srcb, tgtb, stepsz, S, 1, Hd,
                                                                  quad=quad), reps)
         l2 = l2_read_peak(dev)
+        red = reduction_peak(dev)
         times = {"fwd": [], "fwd_learned": [], "bwd": [], "fwd_plain_layout": [], "bwd_plain_layout": [],
                  "learned_windows": [], "bwd_direct": []}
         for i in range(reps + 1):
@@ -497,6 +498,12 @@ def run_ours(args, world, rank, local):
         "learned_windows_ms": round(statistics.median(times["learned_windows"]), 3),
         "fwd_gsamples_per_s": round(n_samp / fwd_s / 1e9, 2),
         "bwd_gsamples_per_s": round(n_samp / kern_s / 1e9, 2),
+        # the scatter's two 16-byte reductions per sample alone, into an
+        # L2-resident array (library probe, this run): the ceiling the
+        # adjoint's sample rate is bound by
+        "reduction_peak_gsamples_per_s": red["gsamples_per_s"],
+        "reduction_peak_how": red["how"],
+        "reduction_frac": round(n_samp / kern_s / 1e9 / red["gsamples_per_s"], 4) if red["gsamples_per_s"] else None,
         "fwd_demand_l2_frac": round(fwd_bytes / (fwd_kernel_ms / 1e3) / 1e9 / l2["gbs"], 4) if l2["gbs"] else None,
         "plain_layout_fwd_ms": round(statistics.median(times["fwd_plain_layout"]), 3),
         "plain_layout_bwd_ms": round(statistics.median(times["bwd_plain_layout"]), 3),
@@ -808,6 +815,47 @@ def l2_read_peak(dev, sizes_mib=(16, 32, 48), passes=256, reps=10, warm_ms=100.0
     sizes = "/".join(str(m) for m in sizes_mib)
     return {"gbs": round(best, 1), "how": f"{sizes} MiB buffers each read {passes}x with ld.global.cg by 4 CTAs x 512 "
             f"threads per SM, best of {reps} per size after ~{warm_ms:.0f} ms of warm-up launches, CUDA events"}
+
+
+def reduction_peak(dev, mib=64, iters=512, reps=10, warm_ms=100.0):
+    """Measured rate (G samples/s) of the volume-gradient scatter's pattern
+    alone: the library's probe has every warp scatter an 8 x 4 patch of
+    neighbouring cells as two 16-byte reductions per sample into an
+    L2-resident quad array; best of `reps` launches after ~`warm_ms` of
+    warm-up, CUDA events."""
+    import ctypes
+
+    from nanodrr_gb300 import _ffi
+
+    lib = _ffi.load()
+    buf = torch.zeros(mib << 20, dtype=torch.uint8, device=dev)
+    threads = ctypes.c_int32(0)
+    stream = torch.cuda.current_stream(dev).cuda_stream
+
+    def launch():
+        _ffi.check(lib.ndrr_reduce_probe(ctypes.c_void_p(buf.data_ptr()), ctypes.c_uint64(buf.numel()), iters,
+                                         ctypes.byref(threads), ctypes.c_void_p(stream)), "ndrr_reduce_probe")
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    launch()
+    e1.record()
+    torch.cuda.synchronize()
+    for _ in range(max(3, min(1000, int(warm_ms / max(e0.elapsed_time(e1), 1e-3))))):
+        launch()
+    torch.cuda.synchronize()
+    best = 0.0
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        launch()
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, threads.value * iters / (e0.elapsed_time(e1) / 1e3) / 1e9)
+    del buf
+    return {"gsamples_per_s": round(best, 1),
+            "how": f"{mib} MiB quad array, {threads.value} threads x {iters} samples, two red.global.add.v4.f32 per "
+                   f"sample, warps as 8 x 4 patches of cells, best of {reps} after ~{warm_ms:.0f} ms of warm-up"}
 
 
 def _rays(sub, rt, k_inv, sdd, det, S):

@@ -531,6 +531,17 @@ NDRR_API int32_t ndrr_set_kernel_events(void* start, void* stop);
  * bytes) is written only in a case real data does not reach. */
 NDRR_API int32_t ndrr_l2_read_probe(const void* buf, uint64_t bytes, int32_t passes, uint32_t* sink, void* stream);
 
+/* Reduction-throughput probe: the volume-gradient scatter's pattern alone.
+ * `buf` (device, 16-byte aligned, >= 5 planes of 512 x 512 x 16 bytes, at
+ * most 4096 planes) is read as quad-entry planes; every thread of 4 CTAs of
+ * 512 per SM adds 1.0 to the four floats of two entries (planes z and z + 1
+ * of its cell: two red.global.add.v4.f32) per iteration, `iters` times, each
+ * warp an 8 x 4 patch of neighbouring cells. `launched_threads` receives the
+ * thread count, so samples = threads x iters; time the call with events. A
+ * buffer of a few tens of MiB stays in L2 and gives the ceiling the adjoint's
+ * scatter is measured against. */
+NDRR_API int32_t ndrr_reduce_probe(void* buf, uint64_t bytes, int32_t iters, int32_t* launched_threads, void* stream);
+
 /* ---- empty-space structures ---------------------------------------------- */
 typedef struct ndrr_occupancy_args {
     uint32_t struct_size;   /* sizeof(ndrr_occupancy_args) */

@@ -162,6 +162,7 @@ SIGNATURES: dict[str, tuple] = {
     "ndrr_set_kernel_events": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_void_p]),
     "ndrr_l2_read_probe": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, ctypes.c_void_p,
                                             ctypes.c_void_p]),
+    "ndrr_reduce_probe": (ctypes.c_int32, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int32, _i32p, ctypes.c_void_p]),
     "ndrr_occupancy_dims": (ctypes.c_int32, [ctypes.c_int32] * 4 + [_i32p] * 3),
     "ndrr_occupancy_build": (ctypes.c_int32, [ctypes.POINTER(OccupancyArgs), ctypes.c_void_p]),
     "ndrr_skip_windows": (ctypes.c_int32, [ctypes.POINTER(RaymarchArgs), ctypes.c_void_p, ctypes.c_void_p]),

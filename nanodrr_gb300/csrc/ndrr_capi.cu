@@ -573,6 +573,23 @@ int32_t ndrr_l2_read_probe(const void* buf, uint64_t bytes, int32_t passes, uint
     return ok();
 }
 
+int32_t ndrr_reduce_probe(void* buf, uint64_t bytes, int32_t iters, int32_t* launched_threads, void* stream) {
+    constexpr uint64_t kPlaneBytes = 512ull * 512ull * 16ull;
+    if (buf == nullptr || launched_threads == nullptr)
+        return fail(NDRR_ERR_INVALID_ARGUMENT, "buf and launched_threads must be non-NULL");
+    if (misaligned(buf, 16) || bytes < 5 * kPlaneBytes || iters < 1)
+        return fail(NDRR_ERR_INVALID_ARGUMENT,
+                    "the reduction probe needs a 16-byte aligned buffer of at least 5 planes of 4 MiB, iters >= 1");
+    const uint64_t planes = bytes / kPlaneBytes;
+    if (planes > 4096) return fail(NDRR_ERR_INVALID_ARGUMENT, "the reduction probe takes at most 4096 planes");
+    const int sms = sm_count_current();
+    *launched_threads = (sms > 0 ? sms : 148) * 4 * 512;
+    const cudaError_t e =
+        ndrr::launch_reduce_probe(buf, (int)planes, iters, sms, reinterpret_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return fail(NDRR_ERR_CUDA, "reduction probe launch failed: %s", cudaGetErrorString(e));
+    return ok();
+}
+
 int32_t ndrr_batch_validate(const ndrr_request* q, int32_t n, int32_t n_classes, int32_t* tiles) {
     if (q == nullptr || tiles == nullptr || n < 0) return fail(NDRR_ERR_INVALID_ARGUMENT, "bad request array");
     if (n_classes < 1 || n_classes > 64) return fail(NDRR_ERR_INVALID_ARGUMENT, "batched n_classes must be 1..64");

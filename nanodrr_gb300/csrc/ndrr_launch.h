@@ -30,6 +30,7 @@ struct KernelEvents {
 KernelEvents& kernel_events();
 cudaError_t launch_l2_probe(const void* buf, unsigned long long bytes, int passes, unsigned* sink, int sm_count,
                             cudaStream_t st);
+cudaError_t launch_reduce_probe(void* buf, int planes, int iters, int sm_count, cudaStream_t st);
 
 LaunchShape choose_shape(const ndrr_raymarch_args& a, int sm_count);
 uint64_t bwd_workspace_bytes(const ndrr_raymarch_args& a, const LaunchShape& ls);

@@ -298,3 +298,13 @@ def test_split_adjoint_rules_are_host_only(lib):
     assert lib.ndrr_raymarch_bwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
     a.vol_quad, a.gvol_mode = 0xA000, 6
     assert lib.ndrr_raymarch_bwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+
+
+def test_reduction_probe_validates_on_the_host(lib):
+    n = ctypes.c_int32(0)
+    plane = 512 * 512 * 16
+    assert lib.ndrr_reduce_probe(None, 5 * plane, 1, ctypes.byref(n), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert lib.ndrr_reduce_probe(0x1008, 5 * plane, 1, ctypes.byref(n), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert lib.ndrr_reduce_probe(0x1000, 4 * plane, 1, ctypes.byref(n), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert lib.ndrr_reduce_probe(0x1000, 5 * plane, 0, ctypes.byref(n), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
+    assert lib.ndrr_reduce_probe(0x1000, 5 * plane, 1, None, None) == _ffi.NDRR_ERR_INVALID_ARGUMENT

@@ -679,3 +679,25 @@ def test_labelled_quad_is_the_render_path_for_16_bit_per_label_volumes():
         plain = nd.render(sub, k_inv, rt, sdd, 32, 32, n_samples=300)
     assert rel_maxabs(out.float(), plain.float()) < 1e-2  # bf16 output rounding of fp32 sums
     assert torch.equal(out.float().sum(1).abs() > 0, plain.float().sum(1).abs() > 0)
+
+
+def test_measurement_probes_run_and_count():
+    """The library's probes behind the bench's roofline: the reduction probe
+    adds 1.0 to four floats of two quad entries per thread and iteration
+    (the total is exact), the L2 read probe and the kernel-event hook run
+    without touching results."""
+    lib = _ffi.load()
+    buf = torch.zeros(6 * 512 * 512 * 4, dtype=torch.float32, device=DEV)  # 6 planes of quad entries
+    n = ctypes.c_int32(0)
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = lib.ndrr_reduce_probe(ctypes.c_void_p(buf.data_ptr()), ctypes.c_uint64(buf.numel() * 4), 3, ctypes.byref(n),
+                               ctypes.c_void_p(stream))
+    assert rc == _ffi.NDRR_OK
+    torch.cuda.synchronize()
+    assert n.value > 0 and float(buf.double().sum()) == n.value * 3 * 2 * 4
+    sink = torch.zeros(1, dtype=torch.int32, device=DEV)
+    src = torch.ones(1 << 20, dtype=torch.uint8, device=DEV)
+    assert lib.ndrr_l2_read_probe(ctypes.c_void_p(src.data_ptr()), ctypes.c_uint64(src.numel()), 2,
+                                  ctypes.c_void_p(sink.data_ptr()), ctypes.c_void_p(stream)) == _ffi.NDRR_OK
+    torch.cuda.synchronize()
+    assert int(sink.item()) == 0
