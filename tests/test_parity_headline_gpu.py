@@ -21,7 +21,9 @@ analytic backward) on the same float32 inputs cast to float64:
     and bf16 (the reference's channel-sum rule, tests/drr/test_fused.py:
     56-65: channel sum within the tolerance, fewer than 0.1 % of rays with a
     channel beyond it; bf16 within 1e-2);
-  - a 1024^2 detector at 1000 samples per ray with the learned proposal.
+  - a 1024^2 detector at 1000 samples per ray with the learned proposal;
+  - the volume stored as bf16 and f16 (within 1e-2) and orthographic rays
+    (within 1e-5).
 
 Rays are subsets (ray lists through render(src=, tgt=)); one check ties the
 subset render to the full-image render of the same poses.
@@ -276,3 +278,39 @@ def test_learned_proposal_1024_detector_within_tolerances(headline):
     finally:
         sub.empty_space = None
         sub._image_hu = keep
+
+
+@pytest.mark.parametrize("dtype", [torch.bfloat16, torch.float16])
+def test_headline_16bit_volume_within_1e2_of_fp64(headline, dtype):
+    """The benchmark volume stored as bf16 / f16 (its quad layout of 16-bit
+    values, fp32 accumulation): the image within 1e-2 of the float64 oracle
+    of the float32 volume."""
+    h = headline
+    s16 = nd.Subject.from_volume(h["sub"]._image_hu.detach()[0, 0].to(dtype), SPACING, convert_to_mu=False)
+    with torch.no_grad():
+        out = nd.render(s16, h["k_inv"], h["rt"], h["sdd"], RAYS // 64, 64, n_samples=S, src=h["src"], tgt=h["tgt"])
+    assert out.dtype == dtype
+    err = _per_pose_rel(out.reshape(4, 1, RAYS).float(), h["ref"])
+    assert err <= 1e-2, err
+
+
+def test_headline_orthographic_image_within_1e5_of_fp64(headline):
+    """Parallel rays of the same pixel subset (src = tgt - (0, 0, sdd), one
+    source per ray) at the benchmark size: the image within 1e-5 of the
+    float64 oracle."""
+    h = headline
+    sub = h["sub"]
+    k_inv, sdd = phantom.detector(sdd=1020.0, pixel=PIXEL, height=DET, width=DET)
+    tgt = h["tgt"]
+    src = tgt.clone()
+    src[..., 2] -= h["sdd"][0]
+    tgt64 = _make_tgt(k_inv.double(), sdd.double(), DET, DET, "cpu", torch.float64)[0][h["idx"]]
+    src64 = tgt64.clone()
+    src64[..., 2] -= float(sdd[0])
+    vol64 = sub._image_hu.detach()[0, 0].double().cpu()
+    ref, _, _ = _oracle(vol64, None, sub.world_to_voxel.double().cpu(), h["rt"].double().cpu(), src64, tgt64, S)
+    with torch.no_grad():
+        out = nd.render(sub, h["k_inv"], h["rt"], h["sdd"], RAYS // 64, 64, n_samples=S, src=src, tgt=tgt)
+    assert float(ref.abs().max()) > 0
+    err = _per_pose_rel(out.reshape(4, 1, RAYS), ref)
+    assert err <= 1e-5, err
