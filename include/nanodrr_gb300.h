@@ -176,9 +176,14 @@ typedef struct ndrr_raymarch_args {
     /* Optional per-ray sample windows [B, N, 2] int32 (first sample, one
      * past the last), as written by ndrr_skip_windows, or NULL. Each ray
      * marches only the samples of its window (intersected with its box-culled
-     * window). It is an empty-space window: valid for the forward and the
-     * pose/camera adjoint, rejected together with need_gvol (the volume
-     * gradient needs every sample) or with skip_mode (one skip at a time). */
+     * window). It is an empty-space window (samples outside it have eight
+     * zero corners): valid for the forward and the pose/camera adjoint, and
+     * with need_gvol for the slab-ordered adjoint of one channel (gvol_mode
+     * 0, 3, 4 with the quad layout), where it only spares the loads of the
+     * samples outside (every sample is still scattered into the volume
+     * gradient; results unchanged), and for gvol_mode 5 (its pose pass).
+     * Rejected with the other need_gvol paths and with skip_mode (one skip
+     * at a time). */
     const int32_t* sample_window;
 
     /* Launch tuning; 0 selects the library default for each. */

@@ -280,8 +280,12 @@ int32_t ndrr_raymarch_bwd_workspace_bytes(const ndrr_raymarch_args* a, uint64_t*
 int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* a, void* stream) {
     int32_t rc = validate_common(a);
     if (rc != NDRR_OK) return rc;
-    // the split adjoint's pose pass honours the skip like a pose-only adjoint
-    const bool split = a->need_gvol && ndrr::choose_shape(*a, 0).split;
+    // the split adjoint's pose pass honours the skip like a pose-only adjoint;
+    // the slab-ordered adjoint of one channel takes sample windows as gather
+    // windows (outside them no corner is loaded; every sample is scattered)
+    const ndrr::LaunchShape ls0 = ndrr::choose_shape(*a, 0);
+    const bool split = a->need_gvol && ls0.split;
+    const bool gated = a->need_gvol && ls0.slab && !ls0.split && a->n_classes == 1;
     if (!a->need_gvol || split) rc = reject_proposal_march(a);
     if (rc != NDRR_OK) return rc;
     if (a->B == 0 || a->N == 0) return ok();
@@ -289,10 +293,11 @@ int32_t ndrr_raymarch_bwd(const ndrr_raymarch_args* a, void* stream) {
     if (!is_float_dtype(a->go_dtype)) return fail(NDRR_ERR_DTYPE, "go dtype %d unsupported", a->go_dtype);
     if (a->gM == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "gM is NULL");
     if (a->need_gvol && a->gvol == nullptr) return fail(NDRR_ERR_INVALID_ARGUMENT, "need_gvol set but gvol is NULL");
-    if (a->need_gvol && a->sample_window != nullptr && !split)
+    if (a->need_gvol && a->sample_window != nullptr && !split && !gated)
         return fail(NDRR_ERR_INVALID_ARGUMENT,
-                    "sample_window with need_gvol needs gvol_mode 5 (split passes): the volume gradient needs every "
-                    "sample, and only the split adjoint's pose pass can use windows");
+                    "sample_window with need_gvol needs the slab-ordered adjoint of one channel (gvol_mode 0, 3 or 4 "
+                    "with the quad layout) or gvol_mode 5: the volume gradient needs every sample, and only those "
+                    "use windows (to skip loads of zero corners)");
     if (a->need_gcam && (a->gsrc == nullptr || a->gtgt == nullptr || a->gstep == nullptr))
         return fail(NDRR_ERR_INVALID_ARGUMENT, "need_gcam set but gsrc/gtgt/gstep is NULL");
     if (a->vol_quad != nullptr && a->need_gvol && a->gvol_quad == nullptr)

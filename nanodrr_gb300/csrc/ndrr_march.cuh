@@ -51,6 +51,8 @@ struct MarchParams {
     float inv_s;
     const float* t_window;
     const int* win;  // per-ray sample windows [B * N][2] or NULL
+    const int* gwin;  // volume-gradient adjoint: gather windows [B * N][2] (samples outside
+                      // them have eight zero corners: scattered without loading) or NULL
     // forward
     void* out;
     void* out_total;
@@ -91,6 +93,7 @@ struct ThreadRay {
     float sx, sy, sz, ex, ey, ez;  // camera-space source and src -> tgt
     int s0, s1;    // this thread's sample chunk
     FixPos f0, fd;  // voxel-space position of sample 0 and the step per sample, 32.32 fixed point
+    int glo, ghi;   // samples whose corners are loaded (all outside have zero corners)
 };
 
 // Fixed-point start and step of a ray: p0 = M [src, 1] and step = M [tgt -
@@ -159,6 +162,8 @@ __device__ __forceinline__ void init_thread_ray(const MarchParams& p, const floa
     }
     tr.s0 = tr.ray.lo;
     tr.s1 = tr.ray.hi;
+    tr.glo = 0;
+    tr.ghi = INT_MAX;
 }
 
 // This thread's share [s0, s1) of the ray's window when K threads split it.
@@ -254,6 +259,14 @@ __device__ __forceinline__ void fetch_cell(const MarchParams& p, float x, float 
     } else {
         load_cell(reinterpret_cast<const VT*>(p.vol), p.D, p.H, p.W, x, y, z, c);
     }
+}
+
+// The cell of a sample known to have eight zero corners: its position and
+// weights, no loads.
+__device__ __forceinline__ void zero_cell(const MarchParams& p, const FixPos& P, Cell& c) {
+    fix_cell(P, p.D, p.H, p.W, c);
+    c.v000 = c.v001 = c.v010 = c.v011 = c.v100 = c.v101 = c.v110 = c.v111 = 0.f;
+    c.cls = 0;
 }
 
 template <typename VT, int QUAD>
@@ -653,14 +666,23 @@ __device__ __forceinline__ void adjoint_samples(const MarchParams& p, const floa
         }
         return;
     }
+    // Samples outside [glo, ghi) have eight zero corners (the window of an
+    // exact skip): no pose terms, so their cells are not loaded, while their
+    // volume-gradient terms (which need no corner values) are scattered.
     for (; s + 1 < s1; s += 2) {
         const float ta = (float)s * p.inv_s, tb = (float)(s + 1) * p.inv_s;
         const FixPos Pa = fix_at(tr, s), Pb = fix_at(tr, s + 1);
         const float ga = sample_go<MULTI>(p, b, tr, go_ray, Pa);
         const float gb = sample_go<MULTI>(p, b, tr, go_ray, Pb);
         Cell ca, cb;
-        fetch_cell<VT, QUAD>(p, Pa, ca);
-        fetch_cell<VT, QUAD>(p, Pb, cb);
+        if (MULTI || (s >= tr.glo && s < tr.ghi))
+            fetch_cell<VT, QUAD>(p, Pa, ca);
+        else
+            zero_cell(p, Pa, ca);
+        if (MULTI || (s + 1 >= tr.glo && s + 1 < tr.ghi))
+            fetch_cell<VT, QUAD>(p, Pb, cb);
+        else
+            zero_cell(p, Pb, cb);
         if (ga != 0.f) adjoint_accumulate<GVOL, GCAM>(m, tr, ta, ga, ca, A, scatter);
         if (gb != 0.f) adjoint_accumulate<GVOL, GCAM>(m, tr, tb, gb, cb, A, scatter);
     }
@@ -670,7 +692,10 @@ __device__ __forceinline__ void adjoint_samples(const MarchParams& p, const floa
         const float gg = sample_go<MULTI>(p, b, tr, go_ray, Pa);
         if (gg != 0.f) {
             Cell cell;
-            fetch_cell<VT, QUAD>(p, Pa, cell);
+            if (MULTI || (s >= tr.glo && s < tr.ghi))
+                fetch_cell<VT, QUAD>(p, Pa, cell);
+            else
+                zero_cell(p, Pa, cell);
             adjoint_accumulate<GVOL, GCAM>(m, tr, t, gg, cell, A, scatter);
         }
     }
@@ -854,7 +879,14 @@ __device__ __forceinline__ void bwd_body(const MarchParams& p, const int tile, c
         // Skipped samples have eight zero corners: no pose or camera terms.
         apply_skip(p, tr, 0.f, 1.f);
     }
-    if constexpr (SLAB) restrict_to_slab(p, tr, cut);
+    if constexpr (SLAB) {
+        restrict_to_slab(p, tr, cut);
+        if (!MULTI && p.gwin && n >= 0) {
+            const int2 w = __ldg(reinterpret_cast<const int2*>(p.gwin) + tr.bn);
+            tr.glo = w.x;
+            tr.ghi = w.y;
+        }
+    }
     chunk_thread_ray(tr, k, p.K);
     float go_ray = 0.f;
     if (!MULTI && n >= 0) go_ray = ld_any_f(p.go, p.go_dtype, tr.bn);

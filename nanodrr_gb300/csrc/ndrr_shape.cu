@@ -26,6 +26,7 @@ MarchParams make_params(const ndrr_raymarch_args& a, const LaunchShape& ls) {
     p.inv_s = 1.0f / (float)(a.n_samples - 1);
     p.t_window = a.t_window;
     p.win = a.sample_window;
+    p.gwin = nullptr;
     p.out = a.out;
     p.out_total = a.out_total;
     p.go = a.go;

@@ -244,7 +244,7 @@ __global__ void __launch_bounds__(256) slab_fill_kernel(const SlabParams s, int 
 
 // ------------------------------------------------------------- the adjoint
 template <typename VT, bool MULTI, bool WARP_AGG, int LAYOUT>
-__global__ void __launch_bounds__(512, 1) raymarch_bwd_slab_kernel(const MarchParams p, const SlabParams s) {
+__global__ void __maxnreg__(96) raymarch_bwd_slab_kernel(const MarchParams p, const SlabParams s) {
     __shared__ int item_sh;
     const int total = s.counters[0];
     while (true) {
@@ -430,6 +430,10 @@ cudaError_t launch_bwd_slab(const ndrr_raymarch_args& a, const LaunchShape& ls, 
                             cudaStream_t st) {
     MarchParams p = p0;
     p.K = 1;  // items are short: one thread per ray
+    // sample windows with a volume gradient gate the gathers only: every
+    // sample of the cull window is scattered
+    p.gwin = p0.win;
+    p.win = nullptr;
     SlabParams s;
     cudaError_t e = slab_setup(a, ls, p, s, st);
     if (e != cudaSuccess) return e;

@@ -418,7 +418,14 @@ def raymarch_backward(
     _check_inputs(vol, lab, M, src, tgt, step, n_samples, n_classes)
     vol, lab, M, src, tgt, step = _prep(vol, lab, M, src, tgt, step)
     B, N, _ = tgt.shape
-    if need_gvol and gvol_mode != _ffi.NDRR_GVOL_SPLIT:
+    # With a volume gradient, sample windows reach the slab-ordered adjoint of
+    # one channel (they spare the loads of zero-corner samples, all of which
+    # are still scattered) and the split adjoint's pose pass; elsewhere every
+    # sample is marched and the skip is dropped.
+    quad_on = quad is not None and quad.numel() > 0
+    slab_like = (gvol_mode in (_ffi.NDRR_GVOL_AUTO, _ffi.NDRR_GVOL_SLAB, _ffi.NDRR_GVOL_SLAB_WARP)
+                 and quad_on and not need_gcam and n_classes == 1)
+    if need_gvol and gvol_mode != _ffi.NDRR_GVOL_SPLIT and not (slab_like and windows is not None):
         skip, windows = None, None
     elif _windows_route(skip):
         if windows is None:
@@ -434,7 +441,6 @@ def raymarch_backward(
         go = go.float()
     empty = torch.empty(0, device=dev, dtype=torch.float32)
     gM = torch.empty(B, 3, 4, device=dev, dtype=torch.float32)
-    quad_on = quad is not None and quad.numel() > 0
     overwrite = False
     if need_gvol:
         if gvol is None:

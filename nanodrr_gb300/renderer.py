@@ -227,8 +227,13 @@ def render_cuda(subject, rt_inv, src, tgt, step_size, n_samples, height, width) 
     quad = cached_quad(subject, vol, lab, C) if layout == "quad" else vol.new_empty(0, dtype=torch.uint8)
     empty = vol.new_empty(0, dtype=torch.uint8)
     if skip is not None:
+        # With a gradient recorded the skip always goes through sample windows
+        # computed ahead of the march (not the in-kernel walk of a fused
+        # occupancy skip): the adjoint reuses them, and with a volume gradient
+        # they spare the loads of zero-corner samples (every sample is still
+        # scattered).
         sk = (skip.grid.grid, skip.grid.cell, skip.packed, int(skip.mode), float(skip.margin),
-              not getattr(skip, "fused", True))
+              (not getattr(skip, "fused", True)) or grad)
     else:
         sk = (empty, 0, empty, 0, 0.0, False)
     slab_mib = int(getattr(subject, "slab_mib", 0))

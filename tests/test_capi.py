@@ -281,17 +281,20 @@ def test_camera_rays_validate_on_the_host(lib):
 
 
 def test_split_adjoint_rules_are_host_only(lib):
-    """Sample windows with a volume gradient only in gvol_mode 5 (its pose
-    pass takes them; the scatter marches every sample); mode 5 needs the
-    quad layout; modes above 5 are refused."""
+    """Sample windows with a volume gradient: taken by the slab-ordered
+    adjoint of one channel (as gather windows) and by gvol_mode 5 (its pose
+    pass), refused by the direct scatter; mode 5 needs the quad layout;
+    modes above 5 are refused."""
     a = _valid_args()
     a.go, a.go_dtype, a.gM = 0x4000, _ffi.NDRR_F32, 0x5000
     a.need_gvol, a.gvol = 1, 0x8000
     a.sample_window = 0x9000
-    a.gvol_mode = _ffi.NDRR_GVOL_SLAB
+    a.gvol_mode = _ffi.NDRR_GVOL_DIRECT
     a.vol_quad, a.gvol_quad = 0xA000, 0xB000
     assert lib.ndrr_raymarch_bwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_INVALID_ARGUMENT
     assert "gvol_mode 5" in lib.ndrr_last_error().decode()
+    a.gvol_mode = _ffi.NDRR_GVOL_SLAB
+    assert lib.ndrr_raymarch_bwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_WORKSPACE  # windows accepted
     a.gvol_mode = _ffi.NDRR_GVOL_SPLIT
     assert lib.ndrr_raymarch_bwd(ctypes.byref(a), None) == _ffi.NDRR_ERR_WORKSPACE  # windows accepted
     a.vol_quad = None

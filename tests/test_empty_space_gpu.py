@@ -269,3 +269,27 @@ def test_split_adjoint_pose_pass_uses_the_skip(fused, dtype):
         one = raymarch_backward(*args, quad=q, gvol_mode=5, tile=(16, 8, 1))
         one_sk = raymarch_backward(*args, quad=q, gvol_mode=5, tile=(16, 8, 1), skip=skip)
         assert torch.equal(one_sk[1], one[1])
+
+
+def test_slab_adjoint_takes_sample_windows_as_gather_windows():
+    """With a volume gradient the slab-ordered adjoint of one channel takes
+    the skip's sample windows as gather windows: samples outside are still
+    scattered (the volume gradient needs every sample) but their zero
+    corners are not loaded. gM bitwise as without windows (the skipped
+    samples' pose terms are exact zeros), the volume gradient equal to
+    rounding; gvol_mode 0 (auto) takes them as well."""
+    from nanodrr_gb300.raymarch import quad_volume, skip_windows
+
+    ph, sub, vol, lab, M, src, tgt, step, n, det, *_ = _case(B=5)
+    q = quad_volume(vol)
+    go = torch.randn(5, 1, det * det, device=DEV, generator=torch.Generator(device=DEV).manual_seed(5))
+    args = (go, vol, vol, M, src, tgt, step, n, 1, det, True, False)
+    full = raymarch_backward(*args, quad=q, gvol_mode=3)
+    win = skip_windows(vol, M, src, tgt, step, n, det, EmptySpace.occupancy(vol, cell=4, fused=False))
+    assert (win[..., 1] - win[..., 0]).sum() < (M.shape[0] * det * det * n)  # something is skipped
+    gated = raymarch_backward(*args, quad=q, gvol_mode=3, windows=win)
+    assert torch.equal(gated[1], full[1])
+    assert rel_maxabs(gated[0], full[0]) < 1e-5
+    auto = raymarch_backward(*args, quad=q, windows=win)
+    assert torch.equal(auto[1], full[1])
+    assert rel_maxabs(auto[0], full[0]) < 1e-5
